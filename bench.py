@@ -1,0 +1,312 @@
+#!/usr/bin/env python3
+"""FLIP liquid substep benchmark (particle-substeps/s on one GB300 per rank).
+
+Default workload (N=1): the large single dam break — bounds [[0,0,0],[1,0.5,0.5]] at
+resolution 256 (256 x 128 x 128 MAC grid, h = 1/256), fill [[0,0,0],[0.25,0.5,0.5]], 8 particles
+per cell seeded with the reference LCG (8,001,504 particles), zero initial velocity, gravity
+-9.81, dt = 1/120 (fps 15, 8 substeps), FLIP 0.95, pressure by PCG with FP64 dot products, FP64
+solution and FP64 restart residuals to relative residual 1e-6.
+
+A step is one substep of that simulation. `value` is device time of K substeps (CUDA events on
+the library's stream, inputs resident in HBM); `e2e` goes through the public C ABI with host
+buffers: per step one pxf_write_particles from pinned memory, one pxf_advance_to_frame of a
+whole frame (`substeps` substeps) and one pxf_read_particles into pinned memory.
+
+--impl reference times the CPU restatement of the reference algorithm (oracle/, OpenMP over all
+host cores) on the same workload; one step = one substep.
+Multi-GPU (torchrun): replicas only — every rank runs its own simulation, no exchange.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # the reference's plain CPU-runnable case: 64 x 32 x 32, red-black GS, 80 iterations
+    "dam64": dict(bounds=((0, 0, 0), (1, 0.5, 0.5)), resolution=64, fill=[((0, 0, 0), (0.25, 0.5, 0.5))],
+                  ppc=8, fps=15.0, substeps=8, solver="gs", iterations=80, lift=False),
+    # large single dam break, precision solver (the metric's headline configuration)
+    "dam256": dict(bounds=((0, 0, 0), (1, 0.5, 0.5)), resolution=256, fill=[((0, 0, 0), (0.25, 0.5, 0.5))],
+                   ppc=8, fps=15.0, substeps=8, solver="pcg", iterations=80, lift=False),
+    # the same grid with the reference's red-black GS (80 iterations)
+    "dam256_gs": dict(bounds=((0, 0, 0), (1, 0.5, 0.5)), resolution=256, fill=[((0, 0, 0), (0.25, 0.5, 0.5))],
+                      ppc=8, fps=15.0, substeps=8, solver="gs", iterations=80, lift=False),
+    # stress double dam break 512 x 256 x 256 (benchmark entry: beyond the scene limits)
+    "dam512": dict(bounds=((0, 0, 0), (2, 1, 1)), resolution=512,
+                   fill=[((0, 0, 0), (0.6, 0.6, 1.0)), ((1.4, 0, 0), (2.0, 0.6, 1.0))],
+                   ppc=8, fps=15.0, substeps=8, solver="gs", iterations=80, lift=True),
+}
+
+
+def env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_fluid(P, cfg):
+    return P.Fluid("bench", [list(cfg["bounds"][0]), list(cfg["bounds"][1])],
+                   [P.FluidBlock(list(a), list(b)) for a, b in cfg["fill"]], resolution=cfg["resolution"],
+                   particles_per_cell=cfg["ppc"], substeps=cfg["substeps"], pressure_iterations=cfg["iterations"])
+
+
+def workload_config(name, cfg, dims, n):
+    return {"workload": f"dam_break_{name}", "grid": list(dims), "particles": n, "ppc": cfg["ppc"],
+            "dt": f"1/{int(cfg['fps'] * cfg['substeps'])}", "pressure": (
+                "pcg_fp64dots_rtol1e-6" if cfg["solver"] == "pcg" else f"rbgs_{cfg['iterations']}"),
+            "seed": 0, "l2": "inputs larger than L2 (particle state 32 B x N, grid fields > 129 MB)",
+            "parallelism": "replicas"}
+
+
+def alg_bytes(stage, N, F, C, Cf):
+    """Algorithmic bytes of one launch of a stage (4 B per face / cell value, 32 B per particle)."""
+    return {
+        "scan+classify": 4 * C + 8 * C + 1 * C,       # counts in, starts + flags out
+        "scatter": 64 * N,                           # particles in and out
+        "p2g": 32 * N + 8 * F,                       # sorted particles in, vel + vel_old out
+        "divergence": 4 * F + 1 * C + 4 * C + 2 * C,  # faces + flags in, divergence + neighbour record out
+        "pressure_rb": 8 * C,                        # half the cells: p of the other colour, div, p out (16C / iteration)
+        "pcg_dir_spmv": 2 * C + 16 * Cf,             # info sweep; r, p in; p', Ap out over system cells
+        "pcg_update": 2 * C + 32 * Cf,               # info sweep; x64 in/out, p, Ap, r in, r out
+        "pcg_restart": 2 * C + 16 * Cf,
+        "project": 8 * F + 8 * C,
+        "g2p": 64 * N + 8 * F,
+    }.get(stage)
+
+
+def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1):
+    """The oracle (CPU restatement of the reference) on all host cores, one substep per step."""
+    import oracle
+    threads = oracle.num_threads(0)
+    fill = [{"min": list(a), "max": list(b)} for a, b in cfg["fill"]]
+    dims, h = oracle.grid([list(cfg["bounds"][0]), list(cfg["bounds"][1])], cfg["resolution"])
+    p = oracle.seed_particles([list(cfg["bounds"][0]), list(cfg["bounds"][1])], cfg["resolution"], fill, cfg["ppc"], 0)
+    dt = oracle.dt_for(cfg["fps"], cfg["substeps"])
+    s = oracle.OracleSim(dims, h, dt, 0.95, list(cfg["bounds"][0]), [0, -9.81, 0], cfg["iterations"], p)
+    if cfg["solver"] == "pcg":
+        s.set_pressure("pcg", rtol=1e-6, max_iter=4000, restart=50)
+    for _ in range(warmup):
+        s.step(sample_substeps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.step(sample_substeps)
+    el = time.perf_counter() - t0
+    n = p.shape[0]
+    return {"value": n * steps * sample_substeps / el, "ms_per_step": 1e3 * el / steps, "cores": threads,
+            "particles": n, "dims": dims}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="dam256", choices=sorted(CONFIGS))
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    rank = env_int("RANK", 0)
+    world = env_int("WORLD_SIZE", 1)
+    local = env_int("LOCAL_RANK", 0)
+    metric = "FLIP particle-substeps/s"
+    unit = "particle-substeps/s"
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        r = cpu_baseline_run(cfg, args.steps, args.warmup)
+        line = {"metric": metric, "value": r["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded dam break, reference LCG seeding)",
+                "config": workload_config(args.config, cfg, r["dims"], r["particles"]),
+                "cpu_baseline": {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": "port",
+                                 "sample": "one full substep of the workload per step, all host threads"},
+                "e2e": {"value": r["value"], "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo", init_method="env://")
+        dist = dist_mod
+
+    from pxlengine_gb300 import build
+    build.build()
+    import numpy as np
+    import pxlengine_gb300 as P
+    from pxlengine_gb300 import _lib as L
+    lib = L.load()
+    if lib.pxf_set_device(local) != 0:
+        raise RuntimeError(lib.pxf_last_error(None).decode())
+
+    fluid = make_fluid(P, cfg)
+    opts = P.make_options(solver=cfg["solver"], rtol=1e-6, max_iter=4000, restart=50,
+                          lift_grid_limits=cfg["lift"])
+    sim = P.FluidState(fluid, fps=cfg["fps"], seed=0, options=opts)
+    N = sim.particle_count()
+    nx, ny, nz = sim.dims
+    C = nx * ny * nz
+    F = (nx + 1) * ny * nz + nx * (ny + 1) * nz + nx * ny * (nz + 1)
+
+    sim.step_timed(args.warmup)
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_wall = time.perf_counter()
+    ms = sim.step_timed(args.steps)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = N * args.steps * world / (ms / 1e3)
+
+    # Roofline of the dominant stage from a stage-by-stage substep (CUDA events on the library's stream).
+    roofline = None
+    stages = []
+    if not args.no_profile:
+        prof = sim.profile_substep()
+        ct = sim.read_grid("cell_type")
+        Cf = int(np.count_nonzero(ct == 1))
+        stages = [{"stage": n, "launches": k, "ms": m} for n, k, m in prof]
+        top = max(prof, key=lambda r: r[2])
+        name, launches, tot = top
+        per_launch = alg_bytes(name, N, F, C, Cf)
+        peaks = {}
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except OSError:
+            pass
+        peak = peaks.get("hbm_gbs", 6800.0)
+        if per_launch:
+            achieved = per_launch / (tot / launches / 1e3) / 1e9
+            roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                        "alg_bytes_per_launch": per_launch, "launches_per_substep": launches,
+                        "avg_launch_us": 1e3 * tot / launches, "share_of_substep": tot / sum(r[2] for r in prof)}
+
+    # End to end through the C ABI with pinned host buffers, one frame per step.
+    e2e = None
+    if args.e2e_steps > 0:
+        hb_in = P.HostBuffer((N, 8))
+        hb_out = P.HostBuffer((N, 8))
+        hb_in.array[:] = sim.read_particles()
+        sim.fluid_advance(0.0)
+        frame = 0
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            frame += 1
+            lib.pxf_write_particles(sim.h, hb_in.ptr, N)
+            rc = lib.pxf_advance_to_frame(sim.h, float(frame))
+            if rc != 0:
+                raise RuntimeError(lib.pxf_last_error(sim.h).decode())
+            lib.pxf_read_particles(sim.h, hb_out.ptr, N)
+        el = time.perf_counter() - t0
+        e2e = {"value": N * cfg["substeps"] * args.e2e_steps * world / el, "unit": unit,
+               "h2d_bytes_per_step": 32 * N, "d2h_bytes_per_step": 32 * N,
+               "step": f"one frame: pxf_write_particles + pxf_advance_to_frame ({cfg['substeps']} substeps) "
+                       "+ pxf_read_particles, pinned host buffers"}
+        hb_in.close()
+        hb_out.close()
+
+    launches_per_substep = sum(s["launches"] for s in stages) if stages else None
+    solver_stats = None
+    if cfg["solver"] == "pcg":
+        it, rel, st = sim.solver_stats()
+        solver_stats = {"pcg_iterations_last_substep": it, "relres": rel, "status": st}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r = cpu_baseline_run(cfg, 1, 0)
+        cpu = {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": "port",
+               "sample": "one full substep of the same workload (from the seeded state), all host threads"}
+
+    if rank == 0:
+        line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, reference LCG seeding)",
+                "config": workload_config(args.config, cfg, sim.dims, N), "roofline": roofline,
+                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": (launches_per_substep * args.steps) if launches_per_substep else None,
+                "solver": solver_stats, "stages": stages, "wall_s_timed": t_wall}
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

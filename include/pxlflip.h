@@ -1,0 +1,205 @@
+/* pxlflip — GB300 (sm_103a) FLIP liquid substep behind a plain C ABI.
+ *
+ * Drop-in for pxlengine's liquid path:
+ *   scene JSON `fluids[]` block        crates/pxl-scene/src/lib.rs:49-129 (types, defaults, grid())
+ *                                      crates/pxl-scene/src/lib.rs:710-735 (validation)
+ *   FluidState::new                    crates/pxl-render/src/fluid.rs:109-228
+ *   Renderer::fluid_advance (sim part) crates/pxl-render/src/fluid.rs:265-306
+ *   the substep kernels                shaders/fluid.slang:87-220
+ *
+ * Conventions: functions return 0 (PXF_OK) or a negative PXF_E* code; the message of the last
+ * failure is available from pxf_last_error(handle) (or pxf_last_error(NULL) for failures that
+ * produced no handle). A handle is used by one host thread at a time and owns one CUDA stream.
+ * The library owns all device memory; callers own every host buffer they pass. Host waits are
+ * bounded (pxf_options.wait_timeout_s) and end in PXF_ETIMEDOUT instead of blocking forever.
+ * No entry point falls back to the CPU: without a usable CUDA device creation fails.
+ */
+#ifndef PXLFLIP_H
+#define PXLFLIP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PXF_API __attribute__((visibility("default")))
+#else
+#define PXF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PXF_OK 0
+#define PXF_EINVAL (-1)     /* invalid argument or scene validation failure */
+#define PXF_ECUDA (-2)      /* CUDA runtime error */
+#define PXF_ENOMEM (-3)     /* device memory could not be allocated / admission refused */
+#define PXF_ETIMEDOUT (-4)  /* a bounded host wait expired */
+#define PXF_ESTATE (-5)     /* call not valid in the handle's current state */
+#define PXF_ENOTFOUND (-6)  /* unknown request id / fluid index out of range */
+
+typedef struct pxf_sim pxf_sim;
+typedef struct pxf_batch pxf_batch;
+typedef struct pxf_server pxf_server;
+typedef struct pxf_snapshot pxf_snapshot;
+
+/* FluidBlock (crates/pxl-scene/src/lib.rs:87-94). */
+typedef struct {
+    float min[3];
+    float max[3];
+    float velocity[3];
+} pxf_fill_block;
+
+/* Fluid (crates/pxl-scene/src/lib.rs:49-85), every simulation field; `materials` is a renderer
+ * concern and is not represented. */
+typedef struct {
+    const char* name;
+    float bounds[2][3];
+    uint32_t resolution;              /* default 64 */
+    const pxf_fill_block* fill;
+    uint32_t fill_count;
+    uint32_t particles_per_cell;      /* default 8 */
+    uint32_t substeps;                /* default 8 */
+    float flip;                       /* default 0.95 */
+    float gravity[3];                 /* default (0, -9.81, 0) */
+    uint32_t pressure_iterations;     /* default 80 */
+    uint32_t surface_refine;          /* default 2 */
+    float particle_radius;            /* default 2 */
+    float warmup;                     /* default 0 */
+    uint32_t max_triangles;           /* default 2,000,000 */
+} pxf_fluid_desc;
+
+#define PXF_PRESSURE_RBGS 0u   /* red-black Gauss-Seidel, pressure_iterations sweeps (reference) */
+#define PXF_PRESSURE_PCG 1u    /* Jacobi PCG: FP32 vectors, FP64 dots, FP64 solution + restarts */
+
+/* Options beyond the reference's Fluid block. pxf_options_init gives the reference behaviour. */
+typedef struct {
+    uint32_t pressure_solver;      /* PXF_PRESSURE_RBGS (default) or PXF_PRESSURE_PCG */
+    double pcg_rtol;               /* relative residual |b - A x| / |b| target, default 1e-6 */
+    uint32_t pcg_max_iter;         /* default 2000 */
+    uint32_t pcg_restart;          /* FP64 residual recomputation period, default 50 */
+    uint32_t lift_grid_limits;     /* 1: accept resolution > 256 and > 16M cells (benchmark entry) */
+    uint32_t keep_p2g_sums;        /* 1: also store the int32 P2G sums (acc, wacc) for inspection */
+    float velocity_sigma;          /* > 0: add N(0, sigma) per velocity component at seeding */
+    uint32_t velocity_seed;        /* seed of that jitter */
+    double wait_timeout_s;         /* bound on every host wait, default 600 s */
+    int32_t p2g_tile;              /* P2G tile shape index (-1: tuned / default) */
+} pxf_options;
+
+PXF_API void pxf_fluid_desc_init(pxf_fluid_desc* desc);
+PXF_API void pxf_options_init(pxf_options* opts);
+
+/* Scene-JSON validation of one fluid (crates/pxl-scene/src/lib.rs:710-735, same messages).
+ * Writes the message to msg (if cap > 0) and returns PXF_EINVAL on failure. */
+PXF_API int pxf_validate(const pxf_fluid_desc* desc, uint32_t index, uint32_t lift_grid_limits, char* msg, size_t cap);
+
+/* Fluid::grid (crates/pxl-scene/src/lib.rs:123-128). */
+PXF_API int pxf_fluid_grid(const pxf_fluid_desc* desc, uint32_t dims[3], float* h);
+
+/* steps_for_frame (crates/pxl-render/src/fluid.rs:234-236). */
+PXF_API uint64_t pxf_steps_for_frame(double warmup, double fps, uint32_t substeps, double frame);
+
+/* FluidState::new (crates/pxl-render/src/fluid.rs:109-228): validates, seeds particles with
+ * the reference LCG (fluid.rs:97-100,121-148) and allocates the simulation on the current
+ * CUDA device. `seed` is render.seed, `fps` is render.fps. */
+PXF_API int pxf_create(const pxf_fluid_desc* desc, uint32_t seed, double fps, pxf_sim** out);
+PXF_API int pxf_create_ex(const pxf_fluid_desc* desc, uint32_t seed, double fps, const pxf_options* opts, pxf_sim** out);
+
+/* Scene::from_json + FluidState::new for fluids[fluid_index] (crates/pxl-scene/src/lib.rs:634-648,
+ * crates/pxl-render/src/lib.rs:204-229): seed and fps come from the scene's `render` block. */
+PXF_API int pxf_create_from_json(const char* scene_json, uint32_t fluid_index, pxf_sim** out);
+PXF_API int pxf_create_from_json_ex(const char* scene_json, uint32_t fluid_index, const pxf_options* opts, pxf_sim** out);
+/* Number of fluids in a scene (after validation), or a negative error code. */
+PXF_API int pxf_scene_fluid_count(const char* scene_json);
+
+/* Renderer::fluid_advance, simulation part (crates/pxl-render/src/fluid.rs:265-306): steps to
+ * the substep count of `frame`, re-seeding from the initial particles on the first call and on
+ * a backwards seek. Returns when the work is complete (bounded wait). */
+PXF_API int pxf_advance_to_frame(pxf_sim* sim, double frame);
+
+/* Enqueue n substeps (fluid.rs:289-303) without waiting; pxf_sync waits (bounded). */
+PXF_API int pxf_step(pxf_sim* sim, uint32_t n_substeps);
+PXF_API int pxf_sync(pxf_sim* sim);
+
+/* FluidState::particle_count (fluid.rs:230-232). */
+PXF_API uint32_t pxf_particle_count(const pxf_sim* sim);
+PXF_API uint64_t pxf_steps_done(const pxf_sim* sim);
+/* Grid dims, cell size and substep dt (FluidPush nx, ny, nz, h, dt; fluid.rs:158-166). */
+PXF_API int pxf_grid_info(const pxf_sim* sim, uint32_t dims[3], float* h, float* dt);
+PXF_API size_t pxf_device_bytes(const pxf_sim* sim);
+/* Device bytes a simulation of this description would allocate (admission control). */
+PXF_API int pxf_estimate_bytes(const pxf_fluid_desc* desc, const pxf_options* opts, uint64_t* bytes);
+
+/* Particles in the reference buffer layout (fluid.slang:9, fluid.rs:143): n records of 8 floats
+ * [x, y, z, 0, vx, vy, vz, 0] in seeding order. n must equal pxf_particle_count. */
+PXF_API int pxf_read_particles(pxf_sim* sim, float* out, size_t n);
+PXF_API int pxf_write_particles(pxf_sim* sim, const float* in, size_t n);
+
+/* Grid buffers of the last completed substep (fluid.slang:23-30). */
+#define PXF_GRID_VEL 1          /* float[F]  velocities after project, faces u, v, w */
+#define PXF_GRID_VEL_OLD 2      /* float[F]  velocities after normalize */
+#define PXF_GRID_ACC 3          /* int32[F]  P2G fixed-point sum of w*v*65536 (keep_p2g_sums) */
+#define PXF_GRID_WACC 4         /* int32[F]  P2G fixed-point sum of w*65536 (keep_p2g_sums) */
+#define PXF_GRID_CELL_COUNT 5   /* uint32[C] particles per cell at the last P2G */
+#define PXF_GRID_CELL_TYPE 6    /* uint32[C] 0 air, 1 fluid, 2 solid */
+#define PXF_GRID_PRESSURE 7     /* float[C] */
+#define PXF_GRID_DIVERGENCE 8   /* float[C]  divergence before projection */
+#define PXF_GRID_PRESSURE64 9   /* double[C] FP64 pressure (precision solver only) */
+PXF_API int pxf_read_grid(pxf_sim* sim, int which, void* out, size_t bytes);
+/* Only PXF_GRID_PRESSURE (the warm start of the next solve) is writable. */
+PXF_API int pxf_write_grid(pxf_sim* sim, int which, const void* in, size_t bytes);
+
+/* Precision-solver statistics of the last substep: PCG steps, final FP64 relative residual and
+ * status (0 converged, 1 iteration cap, 2 breakdown, 3 zero right-hand side). */
+PXF_API int pxf_solver_stats(pxf_sim* sim, uint32_t* iterations, double* relres, uint32_t* status);
+
+/* Device state snapshot (particles, pressure warm start, step counter). */
+PXF_API int pxf_snapshot_take(pxf_sim* sim, pxf_snapshot** out);
+PXF_API int pxf_snapshot_restore(pxf_sim* sim, const pxf_snapshot* snap);
+PXF_API void pxf_snapshot_free(pxf_snapshot* snap);
+
+/* ------------------------------------------------------------------ measurement
+ * Device time of n substeps: CUDA events recorded on the simulation's own stream around the
+ * substep graphs, bounded wait. No reference counterpart (the reference times whole frames on
+ * the host, crates/pxl-render/src/lib.rs:234-250). */
+PXF_API int pxf_step_timed(pxf_sim* sim, uint32_t n_substeps, double* device_ms);
+
+/* One substep launched stage by stage (no graph) with CUDA events between the launches on the
+ * simulation's stream. Fills up to cap records; *count receives the number of stages. */
+typedef struct {
+    char name[32];
+    uint32_t launches;
+    double ms;          /* summed device time of those launches */
+} pxf_stage_time;
+PXF_API int pxf_profile_substep(pxf_sim* sim, pxf_stage_time* out, uint32_t cap, uint32_t* count);
+
+/* Selects the CUDA device of the calling host thread for the simulations it creates (the
+ * library links its own CUDA runtime, so a caller's runtime setting does not carry over). */
+PXF_API int pxf_set_device(int device);
+
+/* Page-locked host memory for fast particle transfers (cudaMallocHost / cudaFreeHost). */
+PXF_API int pxf_host_alloc(size_t bytes, void** out);
+PXF_API void pxf_host_free(void* p);
+
+PXF_API void pxf_destroy(pxf_sim* sim);
+PXF_API const char* pxf_last_error(const pxf_sim* sim);
+
+/* ------------------------------------------------------------------ batched form
+ * Many simulations with uneven grids advance together: every stage is one launch over a packed
+ * multi-grid work index and a whole substep is one CUDA graph launch. No reference counterpart
+ * (the reference steps each FluidState alone, crates/pxl-render/src/lib.rs:238-247). A
+ * simulation belongs to at most one batch; while it does, step it only through the batch. */
+PXF_API int pxf_batch_create(pxf_batch** out);
+PXF_API int pxf_batch_add(pxf_batch* b, pxf_sim* sim);
+PXF_API int pxf_batch_remove(pxf_batch* b, pxf_sim* sim);
+PXF_API uint32_t pxf_batch_size(const pxf_batch* b);
+PXF_API int pxf_batch_step(pxf_batch* b, uint32_t n_substeps);
+PXF_API int pxf_batch_sync(pxf_batch* b);
+PXF_API void pxf_batch_destroy(pxf_batch* b);
+PXF_API const char* pxf_batch_last_error(const pxf_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PXLFLIP_H */

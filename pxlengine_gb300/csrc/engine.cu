@@ -1,0 +1,1137 @@
+// Host engine behind the C ABI (include/pxlflip.h): simulation state (FluidState,
+// crates/pxl-render/src/fluid.rs:74-94), the per-frame advance (fluid.rs:265-306) and batches.
+//
+// Execution model: every simulation belongs to a batch (its own private batch of one, or a
+// shared pxf_batch). A batch owns a CUDA stream, the device array of SimDev descriptors and the
+// work index of each stage, and one instantiated CUDA graph that performs a whole substep for
+// all its simulations:
+//   scan+classify (3) -> scatter -> P2G -> divergence -> pressure -> project -> G2P
+// The red-black pressure loop is unrolled into the graph (2 x iterations launches); the
+// precision solver's loop is a conditional while-node whose body runs until every simulation
+// has converged, so no host round trip happens inside a substep.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/pxlflip.h"
+#include "engine.h"
+#include "pxf_device.cuh"
+#include "pxf_kernels.h"
+#include "scene.h"
+#include "seed.h"
+
+using namespace pxf;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_global_error(int code, const std::string& m) {
+    g_last_error = m;
+    return code;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+// --------------------------------------------------------------------------------- batch
+namespace pxf {
+
+struct BatchImpl {
+    std::vector<pxf_sim*> sims;
+    cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;         // body capture of the conditional node
+    SimDev* d_sims = nullptr;
+    uint32_t* d_base = nullptr;
+    size_t cap_sims = 0;
+    StageWork w_parts, w_tiles, w_cells, w_half, w_faces, w_chunks;
+    uint32_t max_gs_iters = 0;
+    bool any_gs = false, any_pcg = false;
+    int tile_shape = 0;
+    cudaGraphExec_t exec = nullptr;
+    bool dirty = true;
+    bool cond_ok = true;                 // conditional while-node usable
+    // host-driven fallback for the precision loop
+    cudaGraphExec_t exec_pre = nullptr, exec_body = nullptr, exec_post = nullptr;
+    uint32_t* d_flag = nullptr;
+    uint32_t* h_flag = nullptr;
+    double timeout_s = 600.0;
+    std::string err;
+    bool owned_by_sim = false;
+
+    ~BatchImpl();
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int cuda_fail(cudaError_t e, const char* what) {
+        return fail(PXF_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+    int rebuild();
+    int capture();
+    int record_pre(cudaStream_t st);
+    int record_post(cudaStream_t st);
+    int step(uint32_t n);
+    int wait();
+    void drop_graphs();
+    int profile(pxf_stage_time* out, uint32_t cap, uint32_t* count);
+};
+
+}  // namespace pxf
+
+// --------------------------------------------------------------------------------- simulation
+struct pxf_sim {
+    FluidCfg cfg;
+    pxf_options opts;
+    uint32_t seed = 0;
+    double fps = 24.0;
+    uint32_t dims[3] = {0, 0, 0};
+    float h = 0, dt = 0;
+    SimDev dev{};                 // host copy of the device descriptor
+    SeedPlan plan;
+    void* mem = nullptr;          // one device allocation for every buffer
+    size_t mem_bytes = 0;
+    float4* pos0 = nullptr;       // initial particles (re-seed on rewind, fluid.rs:271-275)
+    float4* vel0 = nullptr;
+    uint64_t steps_done = 0;
+    bool initialized = false;
+    pxf::BatchImpl* batch = nullptr;      // batch that steps this simulation
+    pxf::BatchImpl* own = nullptr;        // private batch of one
+    std::string err;
+
+    int fail(int code, const std::string& m) { err = m; return code; }
+    int cuda_fail(cudaError_t e, const char* what) {
+        return fail(PXF_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+};
+
+struct pxf_snapshot {
+    std::vector<float4> pos, vel;
+    std::vector<float> pressure;
+    std::vector<double> x64;
+    uint64_t steps_done = 0;
+    bool initialized = false;
+    uint32_t np = 0, nc = 0;
+};
+
+struct pxf_batch {
+    pxf::BatchImpl impl;
+};
+
+namespace pxf {
+
+// Byte layout of one simulation's allocation.
+struct Layout {
+    size_t posA, velA, posB, velB, pos0, vel0, vel, vel_old, pressure, div, type, count, start, chunk, info, acc, wacc,
+        x64, r, p0, p1, Ap, partial, pcg, total;
+};
+
+static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o) {
+    const uint64_t nc = uint64_t(n[0]) * n[1] * n[2];
+    const uint64_t nf = uint64_t(n[0] + 1) * n[1] * n[2] + uint64_t(n[0]) * (n[1] + 1) * n[2] + uint64_t(n[0]) * n[1] * (n[2] + 1);
+    const uint64_t nchunks = (nc + kScanChunk - 1) / kScanChunk;
+    Layout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t at = off; off += align256(bytes); return at; };
+    L.posA = take(16ull * np);
+    L.velA = take(16ull * np);
+    // posB and velB are adjacent: together they double as the AoS staging buffer (32 B per particle).
+    L.posB = take(16ull * np);
+    L.velB = L.posB + 16ull * np;
+    off = L.posB + align256(32ull * np);
+    L.pos0 = take(16ull * np);
+    L.vel0 = take(16ull * np);
+    L.vel = take(4 * nf);
+    L.vel_old = take(4 * nf);
+    L.pressure = take(4 * nc);
+    L.div = take(4 * nc);
+    L.type = take(nc);
+    L.count = take(4 * nc);
+    L.start = take(4 * (nc + 1));
+    L.chunk = take(4 * nchunks);
+    L.info = take(2 * nc);
+    L.acc = o.keep_p2g_sums ? take(4 * nf) : 0;
+    L.wacc = o.keep_p2g_sums ? take(4 * nf) : 0;
+    const bool pcg = o.pressure_solver == PXF_PRESSURE_PCG;
+    L.x64 = pcg ? take(8 * nc) : 0;
+    L.r = pcg ? take(4 * nc) : 0;
+    L.p0 = pcg ? take(4 * nc) : 0;
+    L.p1 = pcg ? take(4 * nc) : 0;
+    L.Ap = pcg ? take(4 * nc) : 0;
+    L.partial = pcg ? take(16 * nchunks) : 0;
+    L.pcg = pcg ? take(sizeof(PcgState)) : 0;
+    L.total = off;
+    return L;
+}
+
+BatchImpl::~BatchImpl() {
+    drop_graphs();
+    if (d_sims) cudaFree(d_sims);
+    if (d_base) cudaFree(d_base);
+    if (d_flag) cudaFree(d_flag);
+    if (h_flag) cudaFreeHost(h_flag);
+    if (side) cudaStreamDestroy(side);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void BatchImpl::drop_graphs() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (exec_pre) cudaGraphExecDestroy(exec_pre);
+    if (exec_body) cudaGraphExecDestroy(exec_body);
+    if (exec_post) cudaGraphExecDestroy(exec_post);
+    exec = exec_pre = exec_body = exec_post = nullptr;
+}
+
+static inline uint32_t cdiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
+
+int BatchImpl::rebuild() {
+    cudaError_t e;
+    if (!stream) {
+        if ((e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+        if ((e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+    }
+    drop_graphs();
+    const int n = int(sims.size());
+    if (n == 0) { dirty = false; return PXF_OK; }
+    if (size_t(n) > cap_sims) {
+        if (d_sims) cudaFree(d_sims);
+        if (d_base) cudaFree(d_base);
+        d_sims = nullptr;
+        d_base = nullptr;
+        cap_sims = std::max<size_t>(size_t(n), cap_sims * 2);
+        if ((e = cudaMalloc(&d_sims, cap_sims * sizeof(SimDev))) != cudaSuccess) return cuda_fail(e, "batch table");
+        if ((e = cudaMalloc(&d_base, 6 * (cap_sims + 1) * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "batch index");
+    }
+    tile_shape = p2g_shape_index();
+    for (pxf_sim* sm : sims)
+        if (sm->opts.p2g_tile >= 0 && sm->opts.p2g_tile < kNumP2GShapes) tile_shape = sm->opts.p2g_tile;
+    int shape[3];
+    p2g_shape(tile_shape, shape);
+    std::vector<SimDev> host(n);
+    std::vector<uint32_t> base(6 * (n + 1), 0);
+    max_gs_iters = 0;
+    any_gs = any_pcg = false;
+    timeout_s = 0;
+    for (int i = 0; i < n; i++) {
+        pxf_sim* s = sims[i];
+        host[i] = s->dev;
+        const SimDev& d = s->dev;
+        const uint32_t items[6] = {
+            cdiv(d.np, kElemItem),
+            cdiv(d.nx, shape[0]) * cdiv(d.ny, shape[1]) * cdiv(d.nz, shape[2]),
+            cdiv(d.nc, kElemItem),
+            cdiv(uint64_t((d.nx + 1) / 2) * d.ny * d.nz, kElemItem),
+            cdiv(d.nf, kElemItem),
+            cdiv(d.nc, kScanChunk)};
+        for (int k = 0; k < 6; k++) base[k * (n + 1) + i + 1] = base[k * (n + 1) + i] + items[k];
+        if (d.solver == 0) { any_gs = true; max_gs_iters = std::max(max_gs_iters, d.iterations); }
+        else any_pcg = true;
+        timeout_s = std::max(timeout_s, s->opts.wait_timeout_s);
+    }
+    if (timeout_s <= 0) timeout_s = 600.0;
+    if ((e = cudaMemcpyAsync(d_sims, host.data(), n * sizeof(SimDev), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return cuda_fail(e, "batch table upload");
+    if ((e = cudaMemcpyAsync(d_base, base.data(), base.size() * 4, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return cuda_fail(e, "batch index upload");
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "batch upload");
+    StageWork* ws[6] = {&w_parts, &w_tiles, &w_cells, &w_half, &w_faces, &w_chunks};
+    for (int k = 0; k < 6; k++) {
+        ws[k]->sims = d_sims;
+        ws[k]->base = d_base + k * (n + 1);
+        ws[k]->n_sims = n;
+        ws[k]->total = base[k * (n + 1) + n];
+    }
+    int rc = capture();
+    if (rc) return rc;
+    dirty = false;
+    return PXF_OK;
+}
+
+int BatchImpl::record_pre(cudaStream_t st) {
+    const int n = int(sims.size());
+    cudaError_t e;
+    if ((e = launch_scan(w_chunks, d_sims, n, st)) != cudaSuccess) return cuda_fail(e, "scan");
+    if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
+    if ((e = launch_p2g(w_tiles, tile_shape, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+    if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
+    if (any_gs) {
+        for (uint32_t it = 0; it < max_gs_iters; it++)
+            for (uint32_t parity = 0; parity < 2; parity++)
+                if ((e = launch_pressure_rb(w_half, parity, it, st)) != cudaSuccess) return cuda_fail(e, "pressure");
+    }
+    if (any_pcg && (e = launch_pcg_init(w_chunks, st)) != cudaSuccess) return cuda_fail(e, "pcg init");
+    return PXF_OK;
+}
+
+int BatchImpl::record_post(cudaStream_t st) {
+    cudaError_t e;
+    if (any_pcg && (e = launch_pcg_finish(w_chunks, st)) != cudaSuccess) return cuda_fail(e, "pcg finish");
+    if ((e = launch_project(w_faces, st)) != cudaSuccess) return cuda_fail(e, "project");
+    if ((e = launch_g2p(w_parts, st)) != cudaSuccess) return cuda_fail(e, "g2p");
+    return PXF_OK;
+}
+
+static cudaError_t end_capture_to_exec(cudaStream_t st, cudaGraphExec_t* exec) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    return e;
+}
+
+int BatchImpl::capture() {
+    const int n = int(sims.size());
+    cudaError_t e;
+    if (!any_pcg || cond_ok) {
+        if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return cuda_fail(e, "begin capture");
+        int rc = record_pre(stream);
+        bool cond_failed = false;
+        if (!rc && any_pcg) {
+            // while (any simulation still solving) { body }
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t cg = nullptr;
+            const cudaGraphNode_t* deps = nullptr;
+            size_t nd = 0;
+            cudaGraphConditionalHandle h;
+            // cudaGraphNodeParams holds a union without a default constructor: zeroed raw storage.
+            alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
+            std::memset(np_raw, 0, sizeof(np_raw));
+            cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_raw);
+            cudaGraphNode_t cn;
+            e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &cg, &deps, nullptr, &nd);
+            if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, cudaGraphCondAssignDefault);
+            if (e == cudaSuccess) e = launch_pcg_cond(d_sims, n, h, stream);
+            if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &cg, &deps, nullptr, &nd);
+            if (e == cudaSuccess) {
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = h;
+                np.conditional.type = cudaGraphCondTypeWhile;
+                np.conditional.size = 1;
+                e = cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &np);
+            }
+            if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1, cudaStreamSetCaptureDependencies);
+            if (e == cudaSuccess) {
+                cudaGraph_t body = np.conditional.phGraph_out[0];
+                e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    cudaError_t e1 = launch_pcg_body(w_chunks, side);
+                    cudaError_t e2 = launch_pcg_cond(d_sims, n, h, side);
+                    cudaGraph_t out = body;
+                    cudaError_t e3 = cudaStreamEndCapture(side, &out);
+                    e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+                }
+            }
+            if (e != cudaSuccess) cond_failed = true;
+        }
+        if (!rc && !cond_failed) rc = record_post(stream);
+        cudaGraphExec_t ex = nullptr;
+        e = end_capture_to_exec(stream, &ex);
+        if (!rc && !cond_failed && e == cudaSuccess) {
+            exec = ex;
+            return PXF_OK;
+        }
+        if (ex) cudaGraphExecDestroy(ex);
+        cudaGetLastError();
+        if (rc) return rc;
+        if (!cond_failed && e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+        cond_ok = false;   // fall through to the host-driven precision loop
+    }
+    // Host-driven precision loop: pre graph, body graph (8 steps + flag), post graph.
+    if (!d_flag) {
+        if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+        if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+    }
+    if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cuda_fail(e, "capture");
+    int rc = record_pre(stream);
+    if ((e = end_capture_to_exec(stream, &exec_pre)) != cudaSuccess && !rc) return cuda_fail(e, "graph pre");
+    if (rc) return rc;
+    if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cuda_fail(e, "capture");
+    for (int k = 0; k < 8; k++) launch_pcg_body(w_chunks, stream);
+    launch_pcg_any(d_sims, n, d_flag, stream);
+    cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
+    if ((e = end_capture_to_exec(stream, &exec_body)) != cudaSuccess) return cuda_fail(e, "graph body");
+    if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cuda_fail(e, "capture");
+    rc = record_post(stream);
+    if ((e = end_capture_to_exec(stream, &exec_post)) != cudaSuccess && !rc) return cuda_fail(e, "graph post");
+    return rc;
+}
+
+// Bounded wait on the batch stream.
+int BatchImpl::wait() {
+    if (!stream) return PXF_OK;
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "event");
+    e = cudaEventRecord(ev, stream);
+    if (e != cudaSuccess) { cudaEventDestroy(ev); return cuda_fail(e, "event record"); }
+    const auto t0 = std::chrono::steady_clock::now();
+    int spins = 0;
+    while (true) {
+        e = cudaEventQuery(ev);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) { cudaEventDestroy(ev); return cuda_fail(e, "device work failed"); }
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > timeout_s) {
+            cudaEventDestroy(ev);
+            return fail(PXF_ETIMEDOUT, "device work did not finish within " + std::to_string(timeout_s) + " s");
+        }
+        if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(spins > 4096 ? 500 : 20));
+    }
+    cudaEventDestroy(ev);
+    return PXF_OK;
+}
+
+int BatchImpl::step(uint32_t nsteps) {
+    if (sims.empty() || nsteps == 0) return PXF_OK;
+    if (dirty) {
+        int rc = rebuild();
+        if (rc) return rc;
+    }
+    cudaError_t e;
+    for (uint32_t k = 0; k < nsteps; k++) {
+        if (exec) {
+            if ((e = cudaGraphLaunch(exec, stream)) != cudaSuccess) return cuda_fail(e, "substep launch");
+        } else {
+            if ((e = cudaGraphLaunch(exec_pre, stream)) != cudaSuccess) return cuda_fail(e, "substep launch");
+            for (uint32_t guard = 0; guard < 1u << 20; guard++) {
+                if ((e = cudaGraphLaunch(exec_body, stream)) != cudaSuccess) return cuda_fail(e, "pcg launch");
+                int rc = wait();
+                if (rc) return rc;
+                if (*h_flag == 0) break;
+            }
+            if ((e = cudaGraphLaunch(exec_post, stream)) != cudaSuccess) return cuda_fail(e, "substep launch");
+        }
+    }
+    for (pxf_sim* s : sims) s->steps_done += nsteps;
+    return PXF_OK;
+}
+
+// One substep launched stage by stage with events between the launches (eager, no graph).
+int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
+    if (dirty) {
+        int rc = rebuild();
+        if (rc) return rc;
+    }
+    struct Rec { const char* name; uint32_t launches; double ms; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> evs;
+    auto ev = [&]() {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, stream);
+        evs.push_back(e);
+        return evs.size() - 1;
+    };
+    std::vector<std::pair<size_t, size_t>> spans;   // event index pairs per record
+    std::vector<int> owner;
+    auto add = [&](const char* name, size_t a, size_t b) {
+        int k = -1;
+        for (size_t i = 0; i < recs.size(); i++) if (std::strcmp(recs[i].name, name) == 0) k = int(i);
+        if (k < 0) { recs.push_back({name, 0, 0.0}); k = int(recs.size() - 1); }
+        recs[k].launches++;
+        spans.push_back({a, b});
+        owner.push_back(k);
+    };
+    const int n = int(sims.size());
+    cudaError_t e;
+    size_t t0 = ev();
+    if ((e = launch_scan(w_chunks, d_sims, n, stream)) != cudaSuccess) return cuda_fail(e, "scan");
+    size_t t1 = ev(); add("scan+classify", t0, t1);
+    if ((e = launch_scatter(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "scatter");
+    size_t t2 = ev(); add("scatter", t1, t2);
+    if ((e = launch_p2g(w_tiles, tile_shape, stream)) != cudaSuccess) return cuda_fail(e, "p2g");
+    size_t t3 = ev(); add("p2g", t2, t3);
+    if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
+    size_t t4 = ev(); add("divergence", t3, t4);
+    size_t prev = t4;
+    if (any_gs) {
+        for (uint32_t it = 0; it < max_gs_iters; it++)
+            for (uint32_t parity = 0; parity < 2; parity++) {
+                if ((e = launch_pressure_rb(w_half, parity, it, stream)) != cudaSuccess) return cuda_fail(e, "pressure");
+                size_t t = ev(); add("pressure_rb", prev, t); prev = t;
+            }
+    }
+    if (any_pcg) {
+        if (!d_flag) {
+            if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+            if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+        }
+        if ((e = launch_pcg_init(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
+        size_t t = ev(); add("pcg_init+restart", prev, t); prev = t;
+        for (uint32_t guard = 0; guard < 100000; guard++) {
+            if ((e = launch_pcg_dir_spmv(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t a = ev(); add("pcg_dir_spmv", prev, a);
+            if ((e = launch_pcg_update(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t b = ev(); add("pcg_update", a, b);
+            if ((e = launch_pcg_restart(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t c = ev(); add("pcg_restart", b, c);
+            prev = c;
+            if ((guard & 7) == 7) {
+                launch_pcg_any(d_sims, n, d_flag, stream);
+                cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
+                int rc = wait();
+                if (rc) return rc;
+                size_t d = ev();
+                prev = d;
+                if (*h_flag == 0) break;
+            }
+        }
+        if ((e = launch_pcg_finish(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
+        size_t f = ev(); add("pcg_finish", prev, f); prev = f;
+    }
+    if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
+    size_t t5 = ev(); add("project", prev, t5);
+    if ((e = launch_g2p(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "g2p");
+    size_t t6 = ev(); add("g2p", t5, t6);
+    int rc = wait();
+    if (rc) return rc;
+    for (size_t i = 0; i < spans.size(); i++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, evs[spans[i].first], evs[spans[i].second]);
+        recs[owner[i]].ms += ms;
+    }
+    for (auto& x : evs) cudaEventDestroy(x);
+    for (pxf_sim* s : sims) s->steps_done += 1;
+    *count = uint32_t(recs.size());
+    for (uint32_t i = 0; i < cap && i < recs.size(); i++) {
+        std::snprintf(out[i].name, sizeof(out[i].name), "%s", recs[i].name);
+        out[i].launches = recs[i].launches;
+        out[i].ms = recs[i].ms;
+    }
+    return PXF_OK;
+}
+
+int p2g_shape_index() {
+    static int shape = -2;
+    if (shape == -2) {
+        const char* env = std::getenv("PXF_P2G_TILE");
+        shape = env ? std::atoi(env) : 0;
+        if (shape < 0 || shape >= kNumP2GShapes) shape = 0;
+    }
+    return shape;
+}
+
+}  // namespace pxf
+
+// --------------------------------------------------------------------------------- helpers
+namespace {
+
+int ensure_device(std::string& err) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        err = std::string("no CUDA device available: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+        cudaGetLastError();
+        return PXF_ECUDA;
+    }
+    return PXF_OK;
+}
+
+int sim_bin(pxf_sim* s, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(s->dev.count, 0, size_t(s->dev.nc) * 4, st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "clear counts");
+    // A private one-simulation work index for the binning launch.
+    StageWork w;
+    w.sims = s->own->d_sims;
+    w.base = s->own->d_base;   // stage 0 (particles) of the private batch
+    w.n_sims = 1;
+    w.total = cdiv(s->dev.np, kElemItem);
+    if ((e = launch_bin(w, st)) != cudaSuccess) return s->cuda_fail(e, "bin");
+    return PXF_OK;
+}
+
+// Restores the initial particles (fluid.rs:271-275).
+int sim_reset_particles(pxf_sim* s, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(s->dev.posA, s->pos0, 16ull * s->dev.np, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->dev.velA, s->vel0, 16ull * s->dev.np, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "reset particles");
+    return sim_bin(s, st);
+}
+
+cudaStream_t sim_stream(pxf_sim* s) { return s->batch ? s->batch->stream : s->own->stream; }
+
+// Waits for all work queued on the simulation's batch.
+int sim_wait(pxf_sim* s) {
+    BatchImpl* b = s->batch ? s->batch : s->own;
+    int rc = b->wait();
+    if (rc) return s->fail(rc, b->err);
+    return PXF_OK;
+}
+
+int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_options* optsp, pxf_sim** out) {
+    if (!out) return set_global_error(PXF_EINVAL, "out is NULL");
+    *out = nullptr;
+    pxf_options opts;
+    if (optsp) opts = *optsp; else pxf_options_init(&opts);
+    std::string msg;
+    if (!validate_fluid(cfg, 0, opts.lift_grid_limits != 0, msg)) return set_global_error(PXF_EINVAL, msg);
+    if (!(fps > 0.0)) return set_global_error(PXF_EINVAL, "render.fps must be > 0");
+    if (opts.pressure_solver > PXF_PRESSURE_PCG) return set_global_error(PXF_EINVAL, "unknown pressure_solver");
+    if (ensure_device(msg)) return set_global_error(PXF_ECUDA, msg);
+
+    std::unique_ptr<pxf_sim> s(new pxf_sim());
+    s->cfg = cfg;
+    s->opts = opts;
+    s->seed = seed;
+    s->fps = fps;
+    fluid_grid(cfg.bounds, cfg.resolution, s->dims, s->h);
+    const float origin[3] = {cfg.bounds[0][0], cfg.bounds[0][1], cfg.bounds[0][2]};
+    if (!seed_plan(origin, s->h, s->dims, cfg.fill.data(), uint32_t(cfg.fill.size()), cfg.particles_per_cell, seed, s->plan))
+        return set_global_error(PXF_EINVAL, "fluid '" + cfg.name + "': fill blocks are not representable");
+    s->plan.sigma = opts.velocity_sigma;
+    s->plan.vseed = opts.velocity_seed;
+    if (s->plan.total == 0)   // fluid.rs:149
+        return set_global_error(PXF_EINVAL, "fluid '" + cfg.name + "': fill blocks contain no grid cells");
+    if (s->plan.total >= 0xffffffffull)
+        return set_global_error(PXF_EINVAL, "fluid '" + cfg.name + "': too many particles");
+    const uint32_t np = uint32_t(s->plan.total);
+    const Layout L = layout_for(np, s->dims, opts);
+
+    SimDev& d = s->dev;
+    d.nx = int(s->dims[0]); d.ny = int(s->dims[1]); d.nz = int(s->dims[2]);
+    d.np = np;
+    d.h = s->h;
+    s->dt = float(1.0 / (fps * double(cfg.substeps)));   // fluid.rs:164
+    d.dt = s->dt;
+    d.flip = cfg.flip;
+    d.inv_h = 1.0f / s->h;                               // fluid.rs:166
+    for (int a = 0; a < 3; a++) { d.o[a] = origin[a]; d.g[a] = cfg.gravity[a]; }
+    d.nu = (s->dims[0] + 1) * s->dims[1] * s->dims[2];
+    d.nv = s->dims[0] * (s->dims[1] + 1) * s->dims[2];
+    d.nw = s->dims[0] * s->dims[1] * (s->dims[2] + 1);
+    d.nf = d.nu + d.nv + d.nw;
+    d.nc = s->dims[0] * s->dims[1] * s->dims[2];
+    d.iterations = cfg.pressure_iterations;
+    d.solver = opts.pressure_solver;
+    d.rtol = opts.pcg_rtol;
+    d.max_iter = opts.pcg_max_iter;
+    d.restart = opts.pcg_restart ? opts.pcg_restart : 50;
+
+    cudaError_t e = cudaMalloc(&s->mem, L.total);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_global_error(PXF_ENOMEM, "fluid '" + cfg.name + "': cannot allocate " + std::to_string(L.total) +
+                                                " bytes of device memory: " + cudaGetErrorString(e));
+    }
+    s->mem_bytes = L.total;
+    char* m = static_cast<char*>(s->mem);
+    d.posA = reinterpret_cast<float4*>(m + L.posA);
+    d.velA = reinterpret_cast<float4*>(m + L.velA);
+    d.posB = reinterpret_cast<float4*>(m + L.posB);
+    d.velB = reinterpret_cast<float4*>(m + L.velB);
+    s->pos0 = reinterpret_cast<float4*>(m + L.pos0);
+    s->vel0 = reinterpret_cast<float4*>(m + L.vel0);
+    d.vel = reinterpret_cast<float*>(m + L.vel);
+    d.vel_old = reinterpret_cast<float*>(m + L.vel_old);
+    d.pressure = reinterpret_cast<float*>(m + L.pressure);
+    d.div = reinterpret_cast<float*>(m + L.div);
+    d.type = reinterpret_cast<uint8_t*>(m + L.type);
+    d.count = reinterpret_cast<uint32_t*>(m + L.count);
+    d.start = reinterpret_cast<uint32_t*>(m + L.start);
+    d.chunk = reinterpret_cast<uint32_t*>(m + L.chunk);
+    d.info = reinterpret_cast<uint16_t*>(m + L.info);
+    d.acc = opts.keep_p2g_sums ? reinterpret_cast<int32_t*>(m + L.acc) : nullptr;
+    d.wacc = opts.keep_p2g_sums ? reinterpret_cast<int32_t*>(m + L.wacc) : nullptr;
+    if (opts.pressure_solver == PXF_PRESSURE_PCG) {
+        d.x64 = reinterpret_cast<double*>(m + L.x64);
+        d.r = reinterpret_cast<float*>(m + L.r);
+        d.p0 = reinterpret_cast<float*>(m + L.p0);
+        d.p1 = reinterpret_cast<float*>(m + L.p1);
+        d.Ap = reinterpret_cast<float*>(m + L.Ap);
+        d.partial = reinterpret_cast<double*>(m + L.partial);
+        d.pcg = reinterpret_cast<PcgState*>(m + L.pcg);
+    }
+
+    s->own = new BatchImpl();
+    s->own->owned_by_sim = true;
+    s->own->sims.push_back(s.get());
+    int rc = s->own->rebuild();
+    if (rc) {
+        std::string m2 = s->own->err;
+        delete s->own;
+        cudaFree(s->mem);
+        return set_global_error(rc, m2);
+    }
+    cudaStream_t st = s->own->stream;
+    // Grid buffers start at zero (the reference leaves them uninitialised, fluid.rs:204).
+    e = cudaMemsetAsync(s->mem, 0, L.total, st);
+    if (e == cudaSuccess) e = launch_seed(s->plan, d.posA, d.velA, s->pos0, s->vel0, st);
+    if (e != cudaSuccess) {
+        delete s->own;
+        cudaFree(s->mem);
+        return set_global_error(PXF_ECUDA, std::string("seeding: ") + cudaGetErrorString(e));
+    }
+    rc = sim_bin(s.get(), st);
+    if (!rc) rc = sim_wait(s.get());
+    if (rc) {
+        std::string m2 = s->err;
+        delete s->own;
+        cudaFree(s->mem);
+        return set_global_error(rc, m2);
+    }
+    *out = s.release();
+    return PXF_OK;
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------------- C ABI
+extern "C" {
+
+void pxf_fluid_desc_init(pxf_fluid_desc* d) {
+    if (!d) return;
+    std::memset(d, 0, sizeof(*d));
+    FluidCfg def;
+    d->name = "";
+    d->resolution = def.resolution;
+    d->particles_per_cell = def.particles_per_cell;
+    d->substeps = def.substeps;
+    d->flip = def.flip;
+    std::memcpy(d->gravity, def.gravity, sizeof(d->gravity));
+    d->pressure_iterations = def.pressure_iterations;
+    d->surface_refine = def.surface_refine;
+    d->particle_radius = def.particle_radius;
+    d->warmup = def.warmup;
+    d->max_triangles = def.max_triangles;
+}
+
+void pxf_options_init(pxf_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->pressure_solver = PXF_PRESSURE_RBGS;
+    o->pcg_rtol = 1e-6;
+    o->pcg_max_iter = 2000;
+    o->pcg_restart = 50;
+    o->wait_timeout_s = 600.0;
+    o->p2g_tile = -1;
+}
+
+int pxf_validate(const pxf_fluid_desc* desc, uint32_t index, uint32_t lift, char* msg, size_t cap) {
+    if (!desc) return PXF_EINVAL;
+    FluidCfg f;
+    f.from_desc(*desc);
+    std::string m;
+    const bool ok = validate_fluid(f, index, lift != 0, m);
+    if (msg && cap) {
+        std::snprintf(msg, cap, "%s", m.c_str());
+    }
+    return ok ? PXF_OK : PXF_EINVAL;
+}
+
+int pxf_fluid_grid(const pxf_fluid_desc* desc, uint32_t dims[3], float* h) {
+    if (!desc || !dims || !h) return PXF_EINVAL;
+    fluid_grid(desc->bounds, desc->resolution, dims, *h);
+    return PXF_OK;
+}
+
+uint64_t pxf_steps_for_frame(double warmup, double fps, uint32_t substeps, double frame) {
+    double v = std::round((warmup + frame / fps) * fps * double(substeps));
+    if (!(v > 0.0)) return 0;   // .max(0.0); NaN saturates to 0 in `as u64`
+    return v >= 18446744073709551615.0 ? UINT64_MAX : uint64_t(v);
+}
+
+int pxf_create(const pxf_fluid_desc* desc, uint32_t seed, double fps, pxf_sim** out) {
+    return pxf_create_ex(desc, seed, fps, nullptr, out);
+}
+
+int pxf_create_ex(const pxf_fluid_desc* desc, uint32_t seed, double fps, const pxf_options* opts, pxf_sim** out) {
+    if (!desc) return set_global_error(PXF_EINVAL, "desc is NULL");
+    FluidCfg f;
+    f.from_desc(*desc);
+    return create_impl(f, seed, fps, opts, out);
+}
+
+int pxf_create_from_json(const char* json, uint32_t index, pxf_sim** out) {
+    return pxf_create_from_json_ex(json, index, nullptr, out);
+}
+
+int pxf_create_from_json_ex(const char* json, uint32_t index, const pxf_options* opts, pxf_sim** out) {
+    SceneFluids sc;
+    std::string msg;
+    if (!parse_scene(json, sc, msg)) return set_global_error(PXF_EINVAL, msg);
+    if (index >= sc.fluids.size())
+        return set_global_error(PXF_ENOTFOUND, "scene has " + std::to_string(sc.fluids.size()) + " fluids, no index " +
+                                                   std::to_string(index));
+    // fps: render.fps as f32 widened to f64 (crates/pxl-render/src/lib.rs:223).
+    return create_impl(sc.fluids[index], sc.seed, double(sc.fps), opts, out);
+}
+
+int pxf_scene_fluid_count(const char* json) {
+    SceneFluids sc;
+    std::string msg;
+    if (!parse_scene(json, sc, msg)) return set_global_error(PXF_EINVAL, msg);
+    return int(sc.fluids.size());
+}
+
+int pxf_advance_to_frame(pxf_sim* s, double frame) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (s->batch && s->batch != s->own) return s->fail(PXF_ESTATE, "simulation is stepped by a batch");
+    const uint64_t target = pxf_steps_for_frame(double(s->cfg.warmup), s->fps, s->cfg.substeps, frame);
+    if (!s->initialized || target < s->steps_done) {
+        int rc = sim_reset_particles(s, s->own->stream);
+        if (rc) return rc;
+        s->steps_done = 0;
+        s->initialized = true;
+    }
+    if (target > s->steps_done) {
+        const uint64_t n = target - s->steps_done;
+        for (uint64_t k = 0; k < n; k += 0x40000000ull) {
+            int rc = s->own->step(uint32_t(std::min<uint64_t>(n - k, 0x40000000ull)));
+            if (rc) return s->fail(rc, s->own->err);
+        }
+    }
+    return sim_wait(s);
+}
+
+int pxf_step(pxf_sim* s, uint32_t n) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (s->batch && s->batch != s->own) return s->fail(PXF_ESTATE, "simulation is stepped by a batch");
+    s->initialized = true;
+    int rc = s->own->step(n);
+    if (rc) return s->fail(rc, s->own->err);
+    return PXF_OK;
+}
+
+int pxf_sync(pxf_sim* s) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    return sim_wait(s);
+}
+
+uint32_t pxf_particle_count(const pxf_sim* s) { return s ? s->dev.np : 0; }
+uint64_t pxf_steps_done(const pxf_sim* s) { return s ? s->steps_done : 0; }
+size_t pxf_device_bytes(const pxf_sim* s) { return s ? s->mem_bytes : 0; }
+
+int pxf_grid_info(const pxf_sim* s, uint32_t dims[3], float* h, float* dt) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (dims) std::memcpy(dims, s->dims, sizeof(s->dims));
+    if (h) *h = s->h;
+    if (dt) *dt = s->dt;
+    return PXF_OK;
+}
+
+int pxf_estimate_bytes(const pxf_fluid_desc* desc, const pxf_options* optsp, uint64_t* bytes) {
+    if (!desc || !bytes) return set_global_error(PXF_EINVAL, "NULL argument");
+    pxf_options opts;
+    if (optsp) opts = *optsp; else pxf_options_init(&opts);
+    FluidCfg f;
+    f.from_desc(*desc);
+    uint32_t n[3];
+    float h;
+    fluid_grid(f.bounds, f.resolution, n, h);
+    SeedPlan plan;
+    const float origin[3] = {f.bounds[0][0], f.bounds[0][1], f.bounds[0][2]};
+    if (!seed_plan(origin, h, n, f.fill.data(), uint32_t(f.fill.size()), f.particles_per_cell, 0, plan))
+        return set_global_error(PXF_EINVAL, "fill blocks are not representable");
+    *bytes = layout_for(uint32_t(std::min<uint64_t>(plan.total, 0xffffffffull)), n, opts).total;
+    return PXF_OK;
+}
+
+int pxf_read_particles(pxf_sim* s, float* out, size_t n) {
+    if (!s || !out) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (n != s->dev.np) return s->fail(PXF_EINVAL, "particle count mismatch");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    cudaStream_t st = sim_stream(s);
+    float4* staging = s->dev.posB;   // posB|velB: 32 B per particle, free between substeps
+    cudaError_t e = launch_gather_aos(s->dev, staging, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, staging, 32ull * n, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "read particles");
+    return sim_wait(s);
+}
+
+int pxf_write_particles(pxf_sim* s, const float* in, size_t n) {
+    if (!s || !in) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (n != s->dev.np) return s->fail(PXF_EINVAL, "particle count mismatch");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    cudaStream_t st = sim_stream(s);
+    float4* staging = s->dev.posB;
+    cudaError_t e = cudaMemcpyAsync(staging, in, 32ull * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_scatter_aos(s->dev, staging, st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "write particles");
+    rc = sim_bin(s, st);
+    if (rc) return rc;
+    s->initialized = true;
+    return sim_wait(s);
+}
+
+int pxf_read_grid(pxf_sim* s, int which, void* out, size_t bytes) {
+    if (!s || !out) return set_global_error(PXF_EINVAL, "NULL argument");
+    const SimDev& d = s->dev;
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    cudaStream_t st = sim_stream(s);
+    cudaError_t e = cudaSuccess;
+    auto need = [&](size_t b) { return bytes == b; };
+    switch (which) {
+        case PXF_GRID_VEL:
+        case PXF_GRID_VEL_OLD:
+            if (!need(4ull * d.nf)) return s->fail(PXF_EINVAL, "size mismatch");
+            e = cudaMemcpyAsync(out, which == PXF_GRID_VEL ? d.vel : d.vel_old, bytes, cudaMemcpyDeviceToHost, st);
+            break;
+        case PXF_GRID_ACC:
+        case PXF_GRID_WACC:
+            if (!d.acc) return s->fail(PXF_ESTATE, "P2G sums are kept only with keep_p2g_sums");
+            if (!need(4ull * d.nf)) return s->fail(PXF_EINVAL, "size mismatch");
+            e = cudaMemcpyAsync(out, which == PXF_GRID_ACC ? d.acc : d.wacc, bytes, cudaMemcpyDeviceToHost, st);
+            break;
+        case PXF_GRID_CELL_COUNT: {
+            if (!need(4ull * d.nc)) return s->fail(PXF_EINVAL, "size mismatch");
+            uint32_t* tmp = nullptr;
+            e = cudaMalloc(&tmp, bytes);
+            if (e == cudaSuccess) e = launch_counts_from_start(d, tmp, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (tmp) cudaFree(tmp);
+            break;
+        }
+        case PXF_GRID_CELL_TYPE: {
+            if (!need(4ull * d.nc)) return s->fail(PXF_EINVAL, "size mismatch");
+            std::vector<uint8_t> t(d.nc);
+            e = cudaMemcpyAsync(t.data(), d.type, d.nc, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e == cudaSuccess) {
+                uint32_t* o = static_cast<uint32_t*>(out);
+                for (uint32_t i = 0; i < d.nc; i++) o[i] = t[i];
+            }
+            break;
+        }
+        case PXF_GRID_PRESSURE:
+        case PXF_GRID_DIVERGENCE:
+            if (!need(4ull * d.nc)) return s->fail(PXF_EINVAL, "size mismatch");
+            e = cudaMemcpyAsync(out, which == PXF_GRID_PRESSURE ? d.pressure : d.div, bytes, cudaMemcpyDeviceToHost, st);
+            break;
+        case PXF_GRID_PRESSURE64:
+            if (!d.x64) return s->fail(PXF_ESTATE, "FP64 pressure exists only with the precision solver");
+            if (!need(8ull * d.nc)) return s->fail(PXF_EINVAL, "size mismatch");
+            e = cudaMemcpyAsync(out, d.x64, bytes, cudaMemcpyDeviceToHost, st);
+            break;
+        default:
+            return s->fail(PXF_EINVAL, "unknown grid buffer");
+    }
+    if (e != cudaSuccess) return s->cuda_fail(e, "read grid");
+    return sim_wait(s);
+}
+
+int pxf_write_grid(pxf_sim* s, int which, const void* in, size_t bytes) {
+    if (!s || !in) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (which != PXF_GRID_PRESSURE) return s->fail(PXF_EINVAL, "only the pressure warm start is writable");
+    const SimDev& d = s->dev;
+    if (bytes != 4ull * d.nc) return s->fail(PXF_EINVAL, "size mismatch");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    cudaStream_t st = sim_stream(s);
+    cudaError_t e = cudaMemcpyAsync(d.pressure, in, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d.x64) {
+        const float* p = static_cast<const float*>(in);
+        std::vector<double> x(d.nc);
+        for (uint32_t i = 0; i < d.nc; i++) x[i] = double(p[i]);
+        e = cudaMemcpyAsync(d.x64, x.data(), 8ull * d.nc, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
+    if (e != cudaSuccess) return s->cuda_fail(e, "write grid");
+    return sim_wait(s);
+}
+
+int pxf_solver_stats(pxf_sim* s, uint32_t* iters, double* relres, uint32_t* status) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (!s->dev.pcg) return s->fail(PXF_ESTATE, "the red-black solver keeps no statistics");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    PcgState st;
+    cudaError_t e = cudaMemcpy(&st, s->dev.pcg, sizeof(st), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cuda_fail(e, "solver stats");
+    if (iters) *iters = st.iters;
+    if (relres) *relres = st.relres;
+    if (status) *status = st.status;
+    return PXF_OK;
+}
+
+int pxf_snapshot_take(pxf_sim* s, pxf_snapshot** out) {
+    if (!s || !out) return set_global_error(PXF_EINVAL, "NULL argument");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    std::unique_ptr<pxf_snapshot> snap(new pxf_snapshot());
+    const SimDev& d = s->dev;
+    snap->np = d.np;
+    snap->nc = d.nc;
+    snap->pos.resize(d.np);
+    snap->vel.resize(d.np);
+    snap->pressure.resize(d.nc);
+    cudaError_t e = cudaMemcpy(snap->pos.data(), d.posA, 16ull * d.np, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(snap->vel.data(), d.velA, 16ull * d.np, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(snap->pressure.data(), d.pressure, 4ull * d.nc, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && d.x64) {
+        snap->x64.resize(d.nc);
+        e = cudaMemcpy(snap->x64.data(), d.x64, 8ull * d.nc, cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess) return s->cuda_fail(e, "snapshot");
+    snap->steps_done = s->steps_done;
+    snap->initialized = s->initialized;
+    *out = snap.release();
+    return PXF_OK;
+}
+
+int pxf_snapshot_restore(pxf_sim* s, const pxf_snapshot* snap) {
+    if (!s || !snap) return set_global_error(PXF_EINVAL, "NULL argument");
+    const SimDev& d = s->dev;
+    if (snap->np != d.np || snap->nc != d.nc) return s->fail(PXF_EINVAL, "snapshot belongs to another simulation shape");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    cudaStream_t st = sim_stream(s);
+    cudaError_t e = cudaMemcpyAsync(d.posA, snap->pos.data(), 16ull * d.np, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.velA, snap->vel.data(), 16ull * d.np, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.pressure, snap->pressure.data(), 4ull * d.nc, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d.x64 && snap->x64.size() == d.nc)
+        e = cudaMemcpyAsync(d.x64, snap->x64.data(), 8ull * d.nc, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return s->cuda_fail(e, "restore");
+    rc = sim_bin(s, st);
+    if (rc) return rc;
+    s->steps_done = snap->steps_done;
+    s->initialized = snap->initialized;
+    return sim_wait(s);
+}
+
+void pxf_snapshot_free(pxf_snapshot* snap) { delete snap; }
+
+int pxf_step_timed(pxf_sim* s, uint32_t n, double* ms) {
+    if (!s || !ms) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (s->batch && s->batch != s->own) return s->fail(PXF_ESTATE, "simulation is stepped by a batch");
+    BatchImpl* b = s->own;
+    if (b->dirty) {
+        int rc = b->rebuild();
+        if (rc) return s->fail(rc, b->err);
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, b->stream);
+    s->initialized = true;
+    int rc = b->step(n);
+    cudaEventRecord(e1, b->stream);
+    if (!rc) rc = b->wait();
+    float t = 0;
+    if (!rc) cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return s->fail(rc, b->err);
+    *ms = double(t);
+    return PXF_OK;
+}
+
+int pxf_profile_substep(pxf_sim* s, pxf_stage_time* out, uint32_t cap, uint32_t* count) {
+    if (!s || !count) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (s->batch && s->batch != s->own) return s->fail(PXF_ESTATE, "simulation is stepped by a batch");
+    s->initialized = true;
+    int rc = s->own->profile(out, cap, count);
+    if (rc) return s->fail(rc, s->own->err);
+    return PXF_OK;
+}
+
+int pxf_set_device(int device) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_global_error(PXF_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    }
+    return PXF_OK;
+}
+
+int pxf_host_alloc(size_t bytes, void** out) {
+    if (!out) return set_global_error(PXF_EINVAL, "out is NULL");
+    cudaError_t e = cudaMallocHost(out, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return set_global_error(PXF_ENOMEM, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    return PXF_OK;
+}
+
+void pxf_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+void pxf_destroy(pxf_sim* s) {
+    if (!s) return;
+    if (s->batch && s->batch != s->own) {
+        BatchImpl* b = s->batch;
+        b->wait();
+        b->sims.erase(std::remove(b->sims.begin(), b->sims.end(), s), b->sims.end());
+        b->dirty = true;
+    }
+    if (s->own) {
+        s->own->wait();
+        delete s->own;
+    }
+    if (s->mem) cudaFree(s->mem);
+    delete s;
+}
+
+const char* pxf_last_error(const pxf_sim* s) { return s ? s->err.c_str() : g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------- batches
+int pxf_batch_create(pxf_batch** out) {
+    if (!out) return set_global_error(PXF_EINVAL, "out is NULL");
+    std::string msg;
+    if (ensure_device(msg)) return set_global_error(PXF_ECUDA, msg);
+    *out = new pxf_batch();
+    return PXF_OK;
+}
+
+int pxf_batch_add(pxf_batch* b, pxf_sim* s) {
+    if (!b || !s) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (s->batch && s->batch != s->own) return b->impl.fail(PXF_ESTATE, "simulation already belongs to a batch");
+    int rc = s->own->wait();
+    if (rc) return b->impl.fail(rc, s->own->err);
+    rc = b->impl.wait();
+    if (rc) return rc;
+    s->batch = &b->impl;
+    s->initialized = true;
+    b->impl.sims.push_back(s);
+    b->impl.dirty = true;
+    return PXF_OK;
+}
+
+int pxf_batch_remove(pxf_batch* b, pxf_sim* s) {
+    if (!b || !s) return set_global_error(PXF_EINVAL, "NULL argument");
+    auto it = std::find(b->impl.sims.begin(), b->impl.sims.end(), s);
+    if (it == b->impl.sims.end()) return b->impl.fail(PXF_ENOTFOUND, "simulation is not in this batch");
+    int rc = b->impl.wait();
+    if (rc) return rc;
+    b->impl.sims.erase(it);
+    s->batch = nullptr;
+    b->impl.dirty = true;
+    return PXF_OK;
+}
+
+uint32_t pxf_batch_size(const pxf_batch* b) { return b ? uint32_t(b->impl.sims.size()) : 0; }
+
+int pxf_batch_step(pxf_batch* b, uint32_t n) {
+    if (!b) return set_global_error(PXF_EINVAL, "batch is NULL");
+    return b->impl.step(n);
+}
+
+int pxf_batch_sync(pxf_batch* b) {
+    if (!b) return set_global_error(PXF_EINVAL, "batch is NULL");
+    return b->impl.wait();
+}
+
+void pxf_batch_destroy(pxf_batch* b) {
+    if (!b) return;
+    b->impl.wait();
+    for (pxf_sim* s : b->impl.sims) s->batch = nullptr;
+    delete b;
+}
+
+const char* pxf_batch_last_error(const pxf_batch* b) { return b ? b->impl.err.c_str() : g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,9 @@
+// Engine internals shared between the host translation units.
+#pragma once
+
+namespace pxf {
+
+// Default P2G tile shape index (PXF_P2G_TILE environment variable, else 0).
+int p2g_shape_index();
+
+}  // namespace pxf

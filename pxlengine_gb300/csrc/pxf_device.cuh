@@ -1,0 +1,104 @@
+// Device-side data model of the FLIP substep: one SimDev per simulation, packed into a device
+// array so that every stage runs as ONE launch over all simulations of a batch (a single drop-in
+// simulation is a batch of one).
+//
+// HBM layout per simulation (x-fastest everywhere, the reference's own indexing,
+// shaders/fluid.slang:43-53):
+//   particles  pos[N] float4 {x, y, z, bits(pid)}  vel[N] float4 {vx, vy, vz, bits(rank)}
+//              A = current state, B = the same particles counting-sorted by cell
+//   faces      vel, vel_old: F floats (u block, then v, then w)
+//   cells      type u8, start u32 (C + 1, exclusive scan of per-cell counts), count u32,
+//              pressure f32, div f32, info u16 (fluid-neighbour mask | non-solid count << 8 |
+//              fluid << 15)
+//   precision  x64 f64, r f32, p (two f32 buffers), Ap f32
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pxf {
+
+enum : uint8_t { AIR = 0, FLUID = 1, SOLID = 2 };   // fluid.slang:40
+
+// Per-simulation scalars of the precision (PCG) solver.
+struct PcgState {
+    double bb;        // |b|^2
+    double rz;        // r.z of the current direction
+    double pAp;
+    double rr;        // recurrence |r|^2
+    double rzn;       // r.z after the update
+    double alpha, beta;
+    double relres;    // last FP64 restart residual / |b|
+    uint32_t iters;   // total PCG steps this solve
+    uint32_t since;   // steps since the last restart
+    uint32_t done;    // 1 when converged, capped or broken down
+    uint32_t fresh;   // 1 right after a restart: next direction p = z
+    uint32_t restart_now;
+    uint32_t status;  // 0 converged, 1 iteration cap, 2 breakdown, 3 zero rhs
+    uint32_t arrive;  // chunks of the current launch that have finished (last-block reduction)
+    uint32_t pbuf;    // which of p0 / p1 holds the current direction
+    uint32_t zero_x;  // zero right-hand side: the solution is x = 0
+    uint32_t pad;
+};
+
+struct SimDev {
+    int nx, ny, nz;
+    uint32_t np;
+    float h, dt, flip, inv_h;
+    float o[3];
+    float g[3];
+    uint32_t nu, nv, nw, nf, nc;
+    uint32_t iterations;     // red-black GS iterations
+    uint32_t solver;         // 0 red-black GS, 1 precision PCG
+    double rtol;
+    uint32_t max_iter, restart;
+    float4 *posA, *velA, *posB, *velB;
+    float *vel, *vel_old, *pressure, *div;
+    uint8_t* type;
+    uint32_t *count, *start, *chunk;
+    uint16_t* info;
+    int32_t *acc, *wacc;     // optional copies of the P2G fixed-point sums
+    double* x64;
+    float *r, *p0, *p1, *Ap;
+    double* partial;         // per-block partial sums of the precision solver
+    PcgState* pcg;
+};
+
+// Work index of one stage over a batch: item i of the stage belongs to simulation s where
+// base[s] <= i < base[s + 1].
+struct Work {
+    const SimDev* sims;
+    const uint32_t* base;
+    int n_sims;
+    uint32_t total;
+};
+
+__device__ __forceinline__ int find_sim(const Work& w, uint32_t item) {
+    int lo = 0, hi = w.n_sims;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(w.base + mid) <= item) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// float -> int32, truncating (cvt.rzi.s32.f32: NaN -> 0, saturating).
+__device__ __forceinline__ int f2i(float x) { return __float2int_rz(x); }
+
+// lerp as the GLSL.std.450 FMix definition: a*(1-t) + b*t (no contraction: built -fmad=false).
+__device__ __forceinline__ float fmix(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Cell of a position, clamped into the grid (fluid.slang:113).
+__device__ __forceinline__ uint32_t cell_of(const SimDev& s, float x, float y, float z) {
+    int i = clampi(f2i(floorf((x - s.o[0]) * s.inv_h)), 0, s.nx - 1);
+    int j = clampi(f2i(floorf((y - s.o[1]) * s.inv_h)), 0, s.ny - 1);
+    int k = clampi(f2i(floorf((z - s.o[2]) * s.inv_h)), 0, s.nz - 1);
+    return uint32_t(i) + uint32_t(s.nx) * (uint32_t(j) + uint32_t(s.ny) * uint32_t(k));
+}
+
+__device__ __forceinline__ bool wall_or_out(const SimDev& s, int i, int j, int k) {
+    return i <= 0 || j <= 0 || k <= 0 || i >= s.nx - 1 || j >= s.ny - 1 || k >= s.nz - 1;
+}
+
+}  // namespace pxf

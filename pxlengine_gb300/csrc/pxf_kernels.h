@@ -1,0 +1,52 @@
+// Host-visible launchers of the FLIP substep kernels (substep.cu, pcg.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pxf {
+
+struct SimDev;
+
+// Device-resident work index of one stage (see Work in pxf_device.cuh).
+struct StageWork {
+    const SimDev* sims = nullptr;
+    const uint32_t* base = nullptr;   // n_sims + 1 entries, device memory
+    int n_sims = 0;
+    uint32_t total = 0;
+};
+
+constexpr uint32_t kScanChunk = 2048;     // cells per scan / precision-solver work item
+constexpr uint32_t kElemItem = 256;       // elements per item of the per-element kernels
+
+int sm_count();
+void p2g_shape(int shape, int out[3]);
+extern const int kNumP2GShapes;
+
+cudaError_t launch_scan(const StageWork& chunks, const SimDev* sims, int n_sims, cudaStream_t st);
+cudaError_t launch_scatter(const StageWork& parts, cudaStream_t st);
+cudaError_t launch_bin(const StageWork& parts, cudaStream_t st);
+cudaError_t launch_p2g(const StageWork& tiles, int shape, cudaStream_t st);
+cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st);
+cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st);
+cudaError_t launch_project(const StageWork& faces, cudaStream_t st);
+cudaError_t launch_g2p(const StageWork& parts, cudaStream_t st);
+
+cudaError_t launch_gather_aos(const SimDev& s, float4* out, cudaStream_t st);
+cudaError_t launch_scatter_aos(const SimDev& s, const float4* in, cudaStream_t st);
+cudaError_t launch_counts_from_start(const SimDev& s, uint32_t* out, cudaStream_t st);
+
+// Precision solver: init (|b|^2, state reset) and one restart, then the loop body
+// (direction + SpMV, update, conditional restart) repeated while any simulation runs; finish
+// writes the FP32 pressure copy.
+cudaError_t launch_pcg_init(const StageWork& chunks, cudaStream_t st);
+cudaError_t launch_pcg_body(const StageWork& chunks, cudaStream_t st);
+cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
+cudaError_t launch_pcg_finish(const StageWork& chunks, cudaStream_t st);
+// The loop body's three kernels, launched one by one (stage profiling).
+cudaError_t launch_pcg_dir_spmv(const StageWork& chunks, cudaStream_t st);
+cudaError_t launch_pcg_update(const StageWork& chunks, cudaStream_t st);
+cudaError_t launch_pcg_restart(const StageWork& chunks, cudaStream_t st);
+// Host-driven fallback: one loop body + a flag telling whether any simulation still runs.
+cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaStream_t st);
+
+}  // namespace pxf

@@ -1,0 +1,662 @@
+// FLIP substep kernels for sm_103a. Every kernel walks a packed work index (pxf_device.cuh) so
+// one launch serves a whole batch of simulations with uneven grids.
+//
+// Stage map against the reference (shaders/fluid.slang, schedule crates/pxl-render/src/fluid.rs:289-303):
+//   clear_grid + cell half of normalize_grid  -> k_scan_chunks / k_scan_sims / k_scan_apply
+//   p2g + face half of normalize_grid + forces -> k_scatter (counting sort) + k_p2g (tiled gather)
+//   compute_divergence                         -> k_divergence
+//   pressure_rb                                -> k_pressure_rb
+//   project                                    -> k_project
+//   g2p_advect                                 -> k_g2p (also bins the advected particle for the
+//                                                 next substep's counting sort)
+//
+// All arithmetic that the reference performs in FP32 is done here in the same order with no
+// contraction (the library is compiled with -fmad=false), so the integer P2G sums, cell counts and
+// flags are bit-exact and the FP32 fields follow the same rounding as the CPU restatement.
+#include "pxf_device.cuh"
+#include "pxf_kernels.h"
+
+namespace pxf {
+
+constexpr uint32_t SCAN_CHUNK = 2048;   // cells per scan work item (256 threads x 8)
+
+// ------------------------------------------------------------------ counting sort: scan + classify
+// Per-chunk sums of the per-cell particle counts.
+__global__ void __launch_bounds__(256) k_scan_chunks(Work w) {
+    __shared__ uint32_t red[8];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t chunk = item - w.base[si];
+        const uint32_t c0 = chunk * SCAN_CHUNK;
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            uint32_t c = c0 + k * 256 + threadIdx.x;
+            if (c < s.nc) sum += s.count[c];
+        }
+        sum = __reduce_add_sync(0xffffffffu, sum);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int k = 0; k < 8; k++) t += red[k];
+            s.chunk[chunk] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// Exclusive scan of the chunk sums, one block per simulation.
+__global__ void __launch_bounds__(1024) k_scan_sims(const SimDev* sims, int n_sims) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t carry;
+    for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
+        const SimDev s = sims[si];
+        const uint32_t nchunks = (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK;
+        if (threadIdx.x == 0) carry = 0;
+        __syncthreads();
+        for (uint32_t base = 0; base < nchunks; base += 1024) {
+            const uint32_t i = base + threadIdx.x;
+            const uint32_t v = i < nchunks ? s.chunk[i] : 0u;
+            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            uint32_t x = v;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= d) x += y;
+            }
+            if (lane == 31) wsum[wid] = x;
+            __syncthreads();
+            if (wid == 0) {
+                uint32_t t = wsum[lane];
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    uint32_t y = __shfl_up_sync(0xffffffffu, t, d);
+                    if (lane >= d) t += y;
+                }
+                wsum[lane] = t;
+            }
+            __syncthreads();
+            const uint32_t before = (wid ? wsum[wid - 1] : 0u) + carry;
+            if (i < nchunks) s.chunk[i] = before + x - v;
+            __syncthreads();
+            if (threadIdx.x == 1023) carry = before + x;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) s.start[s.nc] = carry;
+        __syncthreads();
+    }
+}
+
+// start = exclusive scan of count; count := 0 for the next binning; cell type and the pressure
+// reset of normalize_grid (fluid.slang:125-131).
+__global__ void __launch_bounds__(256) k_scan_apply(Work w) {
+    __shared__ uint32_t wsum[8];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t chunk = item - w.base[si];
+        const uint32_t c0 = chunk * SCAN_CHUNK + threadIdx.x * 8;
+        uint32_t v[8];
+        uint32_t tsum = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            uint32_t c = c0 + k;
+            v[k] = c < s.nc ? s.count[c] : 0u;
+            tsum += v[k];
+        }
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        uint32_t x = tsum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += y;
+        }
+        if (lane == 31) wsum[wid] = x;
+        __syncthreads();
+        uint32_t before = s.chunk[chunk];
+        for (int k = 0; k < wid; k++) before += wsum[k];
+        before += x - tsum;
+        const uint32_t nxy = uint32_t(s.nx) * uint32_t(s.ny);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t c = c0 + k;
+            if (c < s.nc) {
+                s.start[c] = before;
+                before += v[k];
+                s.count[c] = 0;
+                const int i = int(c % uint32_t(s.nx));
+                const int j = int((c / uint32_t(s.nx)) % uint32_t(s.ny));
+                const int kk = int(c / nxy);
+                const uint8_t t = wall_or_out(s, i, j, kk) ? SOLID : (v[k] > 0 ? FLUID : AIR);
+                s.type[c] = t;
+                if (t != FLUID) {
+                    s.pressure[c] = 0.0f;
+                    if (s.x64) s.x64[c] = 0.0;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ counting sort: scatter
+// B[start[cell] + rank] = A. The cell is recomputed from the position with the same expression
+// that produced the rank, so it matches bit for bit.
+__global__ void __launch_bounds__(256) k_scatter(Work w) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t i = (item - w.base[si]) * 256 + threadIdx.x;
+        if (i >= s.np) continue;
+        const float4 P = s.posA[i];
+        const float4 V = s.velA[i];
+        const uint32_t c = cell_of(s, P.x, P.y, P.z);
+        const uint32_t dst = s.start[c] + __float_as_uint(V.w);
+        if (dst < s.np) {   // always true when the ranks come from the last binning
+            s.posB[dst] = P;
+            s.velB[dst] = V;
+        }
+    }
+}
+
+// Binning of the current particles (first substep and after a host write): count + rank.
+__global__ void __launch_bounds__(256) k_bin(Work w) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t i = (item - w.base[si]) * 256 + threadIdx.x;
+        const bool live = i < s.np;
+        uint32_t c = 0xffffffffu;
+        if (live) {
+            const float4 P = s.posA[i];
+            c = cell_of(s, P.x, P.y, P.z);
+        }
+        const unsigned active = __ballot_sync(0xffffffffu, live);
+        if (live) {
+            const unsigned peers = __match_any_sync(active, c);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&s.count[c], uint32_t(__popc(peers)));
+            base = __shfl_sync(peers, base, leader);
+            const uint32_t rank = base + __popc(peers & ((1u << lane) - 1u));
+            s.velA[i].w = __uint_as_float(rank);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ P2G (tiled gather)
+// One work item = one TX x TY x TZ tile of cells. The tile's particles plus a one-cell halo are
+// contiguous per x-row in the sorted array, so each warp streams whole rows. Every particle's
+// 24 face contributions are the reference's int32 fixed-point terms (fluid.slang:97-111); the
+// tile owns its faces, so the integer sums live in shared memory and never touch global atomics.
+// The epilogue is normalize_grid's face half and forces (fluid.slang:119-124, 142-151).
+template <int TX, int TY, int TZ>
+struct P2GTile {
+    static constexpr int FU = (TX + 1) * TY * TZ;
+    static constexpr int FV = TX * (TY + 1) * TZ;
+    static constexpr int FW = TX * TY * (TZ + 1);
+    static constexpr int NF = FU + FV + FW;
+    static constexpr int SMEM = NF * 2 * 4;
+};
+
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(256) k_p2g(Work w) {
+    using T = P2GTile<TX, TY, TZ>;
+    extern __shared__ int smem[];
+    int* sacc = smem;
+    int* swac = smem + T::NF;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t t = item - w.base[si];
+        const int ntx = (s.nx + TX - 1) / TX, nty = (s.ny + TY - 1) / TY;
+        const int x0 = int(t % uint32_t(ntx)) * TX;
+        const int y0 = int((t / uint32_t(ntx)) % uint32_t(nty)) * TY;
+        const int z0 = int(t / uint32_t(ntx * nty)) * TZ;
+        const int n[3] = {s.nx, s.ny, s.nz};
+        const int org[3] = {x0, y0, z0};
+        const int TT[3] = {TX, TY, TZ};
+        // Owned face box per component: full tile, plus the upper boundary face on the own axis
+        // for the last tile along that axis.
+        int E[3][3];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                if (a == c) E[c][a] = (org[a] + TT[a] >= n[a]) ? (n[a] + 1 - org[a]) : TT[a];
+                else E[c][a] = min(TT[a], n[a] - org[a]);
+            }
+        const int sbase[3] = {0, T::FU, T::FU + T::FV};
+        const int sdx[3] = {TX + 1, TX, TX};
+        const int sdy[3] = {TY, TY + 1, TY};
+        for (int i = threadIdx.x; i < T::NF; i += blockDim.x) { sacc[i] = 0; swac[i] = 0; }
+        __syncthreads();
+
+        const float SW = 65536.0f;
+        const int rows_y = TY + 2;
+        const int nrows = (TY + 2) * (TZ + 2);
+        for (int r = warp; r < nrows; r += blockDim.x >> 5) {
+            const int yy = y0 - 1 + r % rows_y, zz = z0 - 1 + r / rows_y;
+            if (yy < 0 || yy >= s.ny || zz < 0 || zz >= s.nz) continue;
+            const int xa = max(x0 - 1, 0), xb = min(x0 + TX, s.nx - 1);
+            const uint32_t rowc = uint32_t(s.nx) * (uint32_t(yy) + uint32_t(s.ny) * uint32_t(zz));
+            const uint32_t pb = s.start[rowc + xa], pe = s.start[rowc + xb + 1];
+            for (uint32_t j = pb + lane; j < pe; j += 32) {
+                const float4 P = s.posB[j];
+                const float4 V = s.velB[j];
+                const float x[3] = {P.x, P.y, P.z};
+                const float vv[3] = {V.x, V.y, V.z};
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    float gq[3];
+                    int b[3];
+                    float wt[3][2];
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        gq[a] = (x[a] - s.o[a]) * s.inv_h - 0.5f;
+                        if (a == c) gq[a] += 0.5f;
+                        b[a] = f2i(floorf(gq[a]));
+                        const float f = gq[a] - float(b[a]);
+                        wt[a][0] = fmix(1.0f - f, f, 0.0f);
+                        wt[a][1] = fmix(1.0f - f, f, 1.0f);
+                        b[a] -= org[a];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 8; k++) {
+                        const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+                        const int lx = b[0] + ox, ly = b[1] + oy, lz = b[2] + oz;
+                        if (lx < 0 || ly < 0 || lz < 0 || lx >= E[c][0] || ly >= E[c][1] || lz >= E[c][2]) continue;
+                        const float wgt = wt[0][ox] * wt[1][oy] * wt[2][oz];
+                        const int si2 = sbase[c] + lx + sdx[c] * (ly + sdy[c] * lz);
+                        atomicAdd(&sacc[si2], f2i(wgt * vv[c] * SW));
+                        atomicAdd(&swac[si2], f2i(wgt * SW));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+
+        // Epilogue: normalize + forces for the owned faces.
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int ex = E[c][0], ey = E[c][1], ez = E[c][2];
+            const int cnt = ex * ey * ez;
+            const uint32_t fdx = uint32_t(s.nx + (c == 0)), fdy = uint32_t(s.ny + (c == 1));
+            const uint32_t fbase = c == 0 ? 0u : (c == 1 ? s.nu : s.nu + s.nv);
+            const float gdt = s.g[c] * s.dt;
+            for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
+                const int lx = idx % ex, ly = (idx / ex) % ey, lz = idx / (ex * ey);
+                const int si2 = sbase[c] + lx + sdx[c] * (ly + sdy[c] * lz);
+                const int a = sacc[si2], wv = swac[si2];
+                const float v = wv > 0 ? float(a) / float(wv) : 0.0f;
+                const int fx = x0 + lx, fy = y0 + ly, fz = z0 + lz;
+                const uint32_t fi = fbase + uint32_t(fx) + fdx * (uint32_t(fy) + fdy * uint32_t(fz));
+                s.vel_old[fi] = v;
+                int lo[3] = {fx, fy, fz};
+                lo[c] -= 1;
+                const bool solid = wall_or_out(s, lo[0], lo[1], lo[2]) || wall_or_out(s, fx, fy, fz);
+                s.vel[fi] = solid ? 0.0f : v + gdt;
+                if (s.acc) { s.acc[fi] = a; s.wacc[fi] = wv; }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ divergence
+// fluid.slang:153-165, plus the per-cell neighbour record used by both pressure solvers.
+__global__ void __launch_bounds__(256) k_divergence(Work w) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t c = (item - w.base[si]) * 256 + threadIdx.x;
+        if (c >= s.nc) continue;
+        const uint32_t nx = uint32_t(s.nx), ny = uint32_t(s.ny), nxy = nx * ny;
+        const int i = int(c % nx), j = int((c / nx) % ny), k = int(c / nxy);
+        float d = 0.0f;
+        uint16_t info = 0;
+        if (s.type[c] == FLUID) {
+            // u faces: (i, j, k) and (i+1, j, k); v faces base nu; w faces base nu + nv.
+            const uint32_t ui = uint32_t(i) + (nx + 1) * (uint32_t(j) + ny * uint32_t(k));
+            const uint32_t vi = s.nu + uint32_t(i) + nx * (uint32_t(j) + (ny + 1) * uint32_t(k));
+            const uint32_t wi = s.nu + s.nv + c;
+            d += s.vel[ui + 1] - s.vel[ui];
+            d += s.vel[vi + nx] - s.vel[vi];
+            d += s.vel[wi + nxy] - s.vel[wi];
+            // Neighbours -x, +x, -y, +y, -z, +z (fluid.slang:173-180). A fluid cell is never on
+            // the wall layer, so every neighbour is inside the grid.
+            const int64_t off[6] = {-1, 1, -int64_t(nx), int64_t(nx), -int64_t(nxy), int64_t(nxy)};
+            uint32_t mask = 0, cnt = 0;
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                const uint8_t t = s.type[int64_t(c) + off[q]];
+                if (t != SOLID) cnt++;
+                if (t == FLUID) mask |= 1u << q;
+            }
+            info = uint16_t(mask | (cnt << 8) | 0x8000u);
+        }
+        s.div[c] = d * s.inv_h;
+        s.info[c] = info;
+    }
+}
+
+// ------------------------------------------------------------------ red-black Gauss-Seidel
+// fluid.slang:167-182: one colour per launch; iteration `it` is skipped by simulations with fewer
+// pressure iterations than the batch maximum.
+__global__ void __launch_bounds__(256) k_pressure_rb(Work w, uint32_t parity, uint32_t it) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        if (it >= s.iterations || s.solver != 0) continue;
+        const uint32_t hx = (uint32_t(s.nx) + 1) >> 1;
+        const uint32_t q = (item - w.base[si]) * 256 + threadIdx.x;
+        const uint32_t row = q / hx;
+        if (row >= uint32_t(s.ny) * uint32_t(s.nz)) continue;
+        const uint32_t ny = uint32_t(s.ny);
+        const uint32_t j = row % ny, k = row / ny;
+        const uint32_t i = 2 * (q - row * hx) + ((j + k + parity) & 1u);
+        if (i >= uint32_t(s.nx)) continue;
+        const uint32_t nx = uint32_t(s.nx), nxy = nx * ny;
+        const uint32_t c = i + nx * row;
+        const uint32_t inf = s.info[c];
+        if (!(inf & 0x8000u)) continue;
+        const float* p = s.pressure;
+        float sum = 0.0f;
+        if (inf & 1u) sum += p[c - 1];
+        if (inf & 2u) sum += p[c + 1];
+        if (inf & 4u) sum += p[c - nx];
+        if (inf & 8u) sum += p[c + nx];
+        if (inf & 16u) sum += p[c - nxy];
+        if (inf & 32u) sum += p[c + nxy];
+        const float cnt = float((inf >> 8) & 7u);
+        if (cnt > 0.0f) s.pressure[c] = (sum - s.div[c] * s.h * s.h / s.dt) / cnt;
+    }
+}
+
+// ------------------------------------------------------------------ project
+// fluid.slang:184-197. With the precision solver the pressure difference comes from the FP64
+// solution.
+__global__ void __launch_bounds__(256) k_project(Work w) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t id = (item - w.base[si]) * 256 + threadIdx.x;
+        if (id >= s.nf) continue;
+        uint32_t c, r, dx, dy;
+        if (id < s.nu) { c = 0; r = id; dx = s.nx + 1; dy = s.ny; }
+        else if (id < s.nu + s.nv) { c = 1; r = id - s.nu; dx = s.nx; dy = s.ny + 1; }
+        else { c = 2; r = id - s.nu - s.nv; dx = s.nx; dy = s.ny; }
+        const int fx = int(r % dx), fy = int((r / dx) % dy), fz = int(r / (dx * dy));
+        int lo[3] = {fx, fy, fz};
+        lo[c] -= 1;
+        if (wall_or_out(s, lo[0], lo[1], lo[2]) || wall_or_out(s, fx, fy, fz)) {
+            s.vel[id] = 0.0f;
+            continue;
+        }
+        const uint32_t nx = uint32_t(s.nx), ny = uint32_t(s.ny);
+        const uint32_t cb = uint32_t(fx) + nx * (uint32_t(fy) + ny * uint32_t(fz));
+        const uint32_t ca = uint32_t(lo[0]) + nx * (uint32_t(lo[1]) + ny * uint32_t(lo[2]));
+        const uint8_t ta = s.type[ca], tb = s.type[cb];
+        if (ta == FLUID || tb == FLUID) {
+            float dp;
+            if (s.solver == 0) {
+                const float pa = ta == FLUID ? s.pressure[ca] : 0.0f;
+                const float pb = tb == FLUID ? s.pressure[cb] : 0.0f;
+                dp = pb - pa;
+            } else {
+                const double pa = ta == FLUID ? s.x64[ca] : 0.0;
+                const double pb = tb == FLUID ? s.x64[cb] : 0.0;
+                dp = float(pb - pa);
+            }
+            s.vel[id] -= s.dt * s.inv_h * dp;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ G2P + advection + binning
+// fluid.slang:67-84 (trilinear sampling with clamped indices) and 199-220.
+__device__ __forceinline__ float sample_face(const SimDev& s, const float* __restrict__ buf, int c, float x,
+                                             float y, float z) {
+    const float xs[3] = {x, y, z};
+    const int n[3] = {s.nx, s.ny, s.nz};
+    float g[3];
+    int b[3], d[3];
+    float wt[3][2];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        g[a] = (xs[a] - s.o[a]) * s.inv_h - 0.5f;
+        if (a == c) g[a] += 0.5f;
+        b[a] = f2i(floorf(g[a]));
+        const float f = g[a] - float(b[a]);
+        wt[a][0] = fmix(1.0f - f, f, 0.0f);
+        wt[a][1] = fmix(1.0f - f, f, 1.0f);
+        d[a] = n[a] + (a == c) - 1;
+    }
+    const uint32_t fdx = uint32_t(d[0] + 1), fdy = uint32_t(d[1] + 1);
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+        const int qx = clampi(b[0] + ox, 0, d[0]);
+        const int qy = clampi(b[1] + oy, 0, d[1]);
+        const int qz = clampi(b[2] + oz, 0, d[2]);
+        const float wgt = wt[0][ox] * wt[1][oy] * wt[2][oz];
+        acc += wgt * __ldg(buf + uint32_t(qx) + fdx * (uint32_t(qy) + fdy * uint32_t(qz)));
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) k_g2p(Work w) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        const uint32_t i = (item - w.base[si]) * 256 + threadIdx.x;
+        const bool live = i < s.np;
+        uint32_t cell = 0xffffffffu;
+        float4 P = make_float4(0, 0, 0, 0), V = make_float4(0, 0, 0, 0);
+        if (live) {
+            P = s.posB[i];
+            V = s.velB[i];
+            const float* fu = s.vel;
+            const float* fv = s.vel + s.nu;
+            const float* fw = s.vel + s.nu + s.nv;
+            const float* ou = s.vel_old;
+            const float* ov = s.vel_old + s.nu;
+            const float* ow = s.vel_old + s.nu + s.nv;
+            const float pic[3] = {sample_face(s, fu, 0, P.x, P.y, P.z), sample_face(s, fv, 1, P.x, P.y, P.z),
+                                  sample_face(s, fw, 2, P.x, P.y, P.z)};
+            const float old[3] = {sample_face(s, ou, 0, P.x, P.y, P.z), sample_face(s, ov, 1, P.x, P.y, P.z),
+                                  sample_face(s, ow, 2, P.x, P.y, P.z)};
+            const float pv[3] = {V.x, V.y, V.z};
+            float x[3] = {P.x, P.y, P.z};
+            float v[3], mid[3];
+            const float hdt = 0.5f * s.dt;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const float fl = pv[a] + pic[a] - old[a];
+                v[a] = fmix(pic[a], fl, s.flip);
+                mid[a] = x[a] + hdt * pic[a];
+            }
+            const float sv[3] = {sample_face(s, fu, 0, mid[0], mid[1], mid[2]),
+                                 sample_face(s, fv, 1, mid[0], mid[1], mid[2]),
+                                 sample_face(s, fw, 2, mid[0], mid[1], mid[2])};
+            const int n[3] = {s.nx, s.ny, s.nz};
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                x[a] += s.dt * sv[a];
+                const float lo = s.o[a] + s.h * 1.001f;
+                const float hi = s.o[a] + s.h * (float(n[a]) - 1.001f);
+                // max(v, 0) / min(v, 0) as (v < 0 ? 0 : v) / (0 < v ? 0 : v): NaN and -0 pass through.
+                if (x[a] < lo) { x[a] = lo; v[a] = v[a] < 0.0f ? 0.0f : v[a]; }
+                if (x[a] > hi) { x[a] = hi; v[a] = 0.0f < v[a] ? 0.0f : v[a]; }
+            }
+            P.x = x[0]; P.y = x[1]; P.z = x[2];
+            V.x = v[0]; V.y = v[1]; V.z = v[2];
+            cell = cell_of(s, x[0], x[1], x[2]);
+        }
+        // Bin for the next substep: warp-aggregated count per cell.
+        const unsigned active = __ballot_sync(0xffffffffu, live);
+        if (live) {
+            const unsigned peers = __match_any_sync(active, cell);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&s.count[cell], uint32_t(__popc(peers)));
+            base = __shfl_sync(peers, base, leader);
+            V.w = __uint_as_float(base + __popc(peers & ((1u << lane) - 1u)));
+            s.posA[i] = P;
+            s.velA[i] = V;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ particle I/O
+// Current particles -> reference AoS layout [x, y, z, 0, vx, vy, vz, 0] in seeding order.
+__global__ void k_gather_aos(SimDev s, float4* __restrict__ out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.np; i += gridDim.x * blockDim.x) {
+        const float4 P = s.posA[i];
+        const float4 V = s.velA[i];
+        const uint32_t pid = __float_as_uint(P.w);
+        if (pid < s.np) {
+            out[2 * pid] = make_float4(P.x, P.y, P.z, 0.0f);
+            out[2 * pid + 1] = make_float4(V.x, V.y, V.z, 0.0f);
+        }
+    }
+}
+
+// Reference AoS layout -> current particles; particle i keeps id i.
+__global__ void k_scatter_aos(SimDev s, const float4* __restrict__ in) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.np; i += gridDim.x * blockDim.x) {
+        const float4 P = in[2 * i];
+        const float4 V = in[2 * i + 1];
+        s.posA[i] = make_float4(P.x, P.y, P.z, __uint_as_float(i));
+        s.velA[i] = make_float4(V.x, V.y, V.z, 0.0f);
+    }
+}
+
+// Per-cell counts of the last binning, from the scan (start[c + 1] - start[c]).
+__global__ void k_counts_from_start(SimDev s, uint32_t* __restrict__ out) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < s.nc; c += gridDim.x * blockDim.x)
+        out[c] = s.start[c + 1] - s.start[c];
+}
+
+// ------------------------------------------------------------------ launchers
+static int g_sm_count = 0;
+
+int sm_count() {
+    if (!g_sm_count) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sm_count <= 0) g_sm_count = 1;
+    }
+    return g_sm_count;
+}
+
+static unsigned grid_for(uint32_t total, int per_sm) {
+    const uint32_t cap = uint32_t(sm_count() * per_sm);
+    return total < cap ? (total ? total : 1u) : cap;
+}
+
+static inline Work mk(const StageWork& sw) {
+    Work w;
+    w.sims = sw.sims;
+    w.base = sw.base;
+    w.n_sims = sw.n_sims;
+    w.total = sw.total;
+    return w;
+}
+
+template <int TX, int TY, int TZ>
+static cudaError_t launch_p2g_t(const StageWork& sw, cudaStream_t st) {
+    using T = P2GTile<TX, TY, TZ>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_p2g<TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, T::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_p2g<TX, TY, TZ>, 256, T::SMEM);
+    if (per_sm < 1) per_sm = 1;
+    k_p2g<TX, TY, TZ><<<grid_for(sw.total, per_sm), 256, T::SMEM, st>>>(mk(sw));
+    return cudaGetLastError();
+}
+
+const int kP2GShapes[][3] = {{32, 8, 8}, {32, 4, 4}, {16, 8, 8}, {64, 4, 4}, {16, 4, 4}};
+const int kNumP2GShapes = 5;
+
+void p2g_shape(int shape, int out[3]) {
+    if (shape < 0 || shape >= kNumP2GShapes) shape = 0;
+    out[0] = kP2GShapes[shape][0];
+    out[1] = kP2GShapes[shape][1];
+    out[2] = kP2GShapes[shape][2];
+}
+
+cudaError_t launch_p2g(const StageWork& sw, int shape, cudaStream_t st) {
+    switch (shape) {
+        case 1: return launch_p2g_t<32, 4, 4>(sw, st);
+        case 2: return launch_p2g_t<16, 8, 8>(sw, st);
+        case 3: return launch_p2g_t<64, 4, 4>(sw, st);
+        case 4: return launch_p2g_t<16, 4, 4>(sw, st);
+        default: return launch_p2g_t<32, 8, 8>(sw, st);
+    }
+}
+
+cudaError_t launch_scan(const StageWork& chunks, const SimDev* sims, int n_sims, cudaStream_t st) {
+    k_scan_chunks<<<grid_for(chunks.total, 8), 256, 0, st>>>(mk(chunks));
+    k_scan_sims<<<n_sims, 1024, 0, st>>>(sims, n_sims);
+    k_scan_apply<<<grid_for(chunks.total, 8), 256, 0, st>>>(mk(chunks));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const StageWork& parts, cudaStream_t st) {
+    k_scatter<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin(const StageWork& parts, cudaStream_t st) {
+    k_bin<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st) {
+    k_divergence<<<grid_for(cells.total, 8), 256, 0, st>>>(mk(cells));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st) {
+    k_pressure_rb<<<grid_for(half_cells.total, 8), 256, 0, st>>>(mk(half_cells), parity, it);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project(const StageWork& faces, cudaStream_t st) {
+    k_project<<<grid_for(faces.total, 8), 256, 0, st>>>(mk(faces));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p(const StageWork& parts, cudaStream_t st) {
+    k_g2p<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_aos(const SimDev& s, float4* out, cudaStream_t st) {
+    k_gather_aos<<<grid_for((s.np + 255) / 256, 8), 256, 0, st>>>(s, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_aos(const SimDev& s, const float4* in, cudaStream_t st) {
+    k_scatter_aos<<<grid_for((s.np + 255) / 256, 8), 256, 0, st>>>(s, in);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_counts_from_start(const SimDev& s, uint32_t* out, cudaStream_t st) {
+    k_counts_from_start<<<grid_for((s.nc + 255) / 256, 8), 256, 0, st>>>(s, out);
+    return cudaGetLastError();
+}
+
+}  // namespace pxf

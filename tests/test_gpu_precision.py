@@ -1,0 +1,70 @@
+"""Precision form: Jacobi PCG with FP32 vectors, FP64 dots, FP64 solution and FP64 restarts,
+against the FP64 oracle solve of the same pressure system."""
+import numpy as np
+import pytest
+
+import oracle
+import pxlengine_gb300 as P
+from gpu_util import DIV_VOLUME_TOL, PCG_RTOL, dam, divergence_after_projection, grids_equal, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _pre_pressure(o):
+    for st in ("clear", "p2g", "normalize", "forces", "divergence"):
+        o.stage(st)
+
+
+@pytest.mark.parametrize("res", [32, 64])
+def test_pcg_against_fp64_oracle(lib, res):
+    f = dam(res=res, ppc=8)
+    opts = P.make_options(solver="pcg", rtol=PCG_RTOL, max_iter=4000, restart=50)
+    with P.FluidState(f, fps=15.0, options=opts) as s:
+        o64 = oracle_for(s, f)
+        o64.set_pressure("pcg64", rtol=1e-12, max_iter=20000)
+        for _ in range(3):
+            # The oracle starts each substep from the GPU's particles, runs the same FP32
+            # pre-pressure stages (bit-exact) and solves the identical system in FP64.
+            o64.write(oracle.PARTICLES, s.read_particles())
+            s.step(1)
+            it, rel, status = s.solver_stats()
+            assert status == 0 and rel <= PCG_RTOL, (it, rel, status)
+            _pre_pressure(o64)
+            grids_equal(s, o64, names=("cell_count", "cell_type", "vel_old", "divergence"))
+            o64.stage("pressure")
+            x64 = o64.read(oracle.PRESSURE64)
+            xg = s.read_grid("pressure64")
+            scale = max(1.0, float(np.max(np.abs(x64))))
+            assert float(np.max(np.abs(xg - x64))) <= 1e-4 * scale
+            vel = s.read_grid("vel")
+            ct = s.read_grid("cell_type")
+            div = divergence_after_projection(vel, ct, s.dims, s.cell)
+            assert float(np.max(np.abs(div))) * s.dt <= DIV_VOLUME_TOL
+
+
+def test_pcg_matches_mixed_oracle_iterations(lib):
+    f = dam(res=32, ppc=4)
+    opts = P.make_options(solver="pcg", rtol=PCG_RTOL, max_iter=4000, restart=50)
+    with P.FluidState(f, fps=15.0, options=opts) as s:
+        om = oracle_for(s, f)
+        om.set_pressure("pcg", rtol=PCG_RTOL, max_iter=4000, restart=50)
+        s.step(1)
+        om.step(1)
+        it_g, rel_g, st_g = s.solver_stats()
+        it_o, rel_o = om.pcg_stats()
+        assert st_g == 0 and rel_g <= PCG_RTOL and rel_o <= PCG_RTOL
+        assert abs(int(it_g) - int(it_o)) <= max(3, it_o // 20)
+        # Everything before the solve is bit-exact; the solution agrees to the solver tolerance.
+        grids_equal(s, om, names=("cell_count", "cell_type", "vel_old", "divergence"))
+        xg = s.read_grid("pressure64")
+        xo = om.read(oracle.PRESSURE64)
+        assert float(np.max(np.abs(xg - xo))) <= 1e-4 * max(1.0, float(np.max(np.abs(xo))))
+
+
+def test_pcg_iteration_cap_reports_status(lib):
+    f = dam(res=32, ppc=4)
+    opts = P.make_options(solver="pcg", rtol=1e-12, max_iter=5, restart=50)
+    with P.FluidState(f, fps=15.0, options=opts) as s:
+        s.step(1)
+        it, rel, status = s.solver_stats()
+        assert status == 1 and it == 5 and rel > 1e-12
