@@ -197,6 +197,67 @@ PXF_API int pxf_batch_step(pxf_batch* b, uint32_t n_substeps);
 PXF_API int pxf_batch_sync(pxf_batch* b);
 PXF_API void pxf_batch_destroy(pxf_batch* b);
 PXF_API const char* pxf_batch_last_error(const pxf_batch* b);
+/* n substeps of the whole batch with their device time (CUDA events on the batch's stream). */
+PXF_API int pxf_batch_step_timed(pxf_batch* b, uint32_t n_substeps, double* device_ms);
+
+/* ------------------------------------------------------------------ serving form
+ * A continuous-batching request loop. Requests (a fluid description + a number of substeps) queue
+ * on submit; every tick retires finished requests (their final particles move to host memory and
+ * their device memory is freed), admits queued requests in arrival order while their estimated
+ * device footprint fits the HBM budget, and advances every active request by one batched substep
+ * (one CUDA graph launch). No reference counterpart: pxlengine runs one scene per process.
+ * Thread safety: submit / cancel / status / take_result / stats may be called from any thread;
+ * tick must be called from one thread at a time (or use pxf_server_start for a worker thread). */
+typedef struct {
+    uint64_t hbm_budget_bytes;     /* default 150e9 */
+    uint32_t max_active;           /* default 256 */
+    uint32_t substeps_per_tick;    /* default 1 */
+    double wait_timeout_s;         /* bound on each tick's device wait, default 600 s */
+} pxf_server_config;
+
+#define PXF_REQ_QUEUED 0
+#define PXF_REQ_RUNNING 1
+#define PXF_REQ_DONE 2
+#define PXF_REQ_CANCELLED 3
+#define PXF_REQ_FAILED 4
+
+typedef struct {
+    int32_t state;                 /* PXF_REQ_* */
+    int32_t error;                 /* PXF_E* when failed */
+    uint32_t substeps_done;
+    uint32_t substeps_total;
+    uint32_t particles;
+    uint64_t device_bytes;
+    double submit_s, admit_s, finish_s;   /* server clock (seconds since creation) */
+} pxf_request_status;
+
+typedef struct {
+    uint64_t ticks;
+    uint64_t submitted, admitted, completed, cancelled, rejected;
+    uint32_t active, queued;
+    uint64_t reserved_bytes, peak_reserved_bytes;
+    double particle_substeps;      /* total particle-substeps advanced */
+    double busy_device_ms;         /* summed device time of the batched substeps */
+    double p50_substep_ms, p99_substep_ms;   /* per-tick device time of one batched substep */
+    double p50_tick_wall_ms, p99_tick_wall_ms;
+    double uptime_s;
+} pxf_server_stats;
+
+PXF_API void pxf_server_config_init(pxf_server_config* cfg);
+PXF_API int pxf_server_create(const pxf_server_config* cfg, pxf_server** out);
+PXF_API int pxf_server_submit(pxf_server* s, const pxf_fluid_desc* desc, uint32_t seed, double fps,
+                              const pxf_options* opts, uint32_t substeps, uint64_t* request_id);
+PXF_API int pxf_server_cancel(pxf_server* s, uint64_t request_id);
+PXF_API int pxf_server_tick(pxf_server* s, uint32_t* active);
+PXF_API int pxf_server_status(pxf_server* s, uint64_t request_id, pxf_request_status* out);
+/* Final particles of a finished request ([x,y,z,0,vx,vy,vz,0] records); releases the request. */
+PXF_API int pxf_server_take_result(pxf_server* s, uint64_t request_id, float* out, size_t n);
+PXF_API int pxf_server_stats_get(pxf_server* s, pxf_server_stats* out);
+/* Worker thread that ticks while requests are queued or active (idle wait is bounded). */
+PXF_API int pxf_server_start(pxf_server* s);
+PXF_API int pxf_server_stop(pxf_server* s);
+PXF_API void pxf_server_destroy(pxf_server* s);
+PXF_API const char* pxf_server_last_error(const pxf_server* s);
 
 #ifdef __cplusplus
 }

@@ -4,4 +4,6 @@ The product is libpxlflip.so (CUDA kernels + C++ host engine behind the C ABI in
 include/pxlflip.h). This package builds it (build.build()) and mirrors the reference's liquid
 interface on top of it (fluid.FluidState, fluid.Fluid, fluid.Batch).
 """
-from .fluid import Batch, Fluid, FluidBlock, FluidError, FluidState, Snapshot, make_options, steps_for_frame  # noqa: F401
+from .serve import Server  # noqa: F401
+from .fluid import (Batch, Fluid, FluidBlock, FluidError, FluidState, HostBuffer, Snapshot,  # noqa: F401
+                    make_options, steps_for_frame)

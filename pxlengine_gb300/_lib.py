@@ -42,6 +42,29 @@ class StageTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint32), ("ms", C.c_double)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active", C.c_uint32), ("substeps_per_tick", C.c_uint32),
+                ("wait_timeout_s", C.c_double)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("substeps_done", C.c_uint32),
+                ("substeps_total", C.c_uint32), ("particles", C.c_uint32), ("device_bytes", C.c_uint64),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("ticks", C.c_uint64), ("submitted", C.c_uint64), ("admitted", C.c_uint64),
+                ("completed", C.c_uint64), ("cancelled", C.c_uint64), ("rejected", C.c_uint64),
+                ("active", C.c_uint32), ("queued", C.c_uint32), ("reserved_bytes", C.c_uint64),
+                ("peak_reserved_bytes", C.c_uint64), ("particle_substeps", C.c_double),
+                ("busy_device_ms", C.c_double), ("p50_substep_ms", C.c_double), ("p99_substep_ms", C.c_double),
+                ("p50_tick_wall_ms", C.c_double), ("p99_tick_wall_ms", C.c_double), ("uptime_s", C.c_double)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
+
+
 def _sig():
     vp = C.c_void_p
     pp = C.POINTER(C.c_void_p)
@@ -90,6 +113,19 @@ def _sig():
         "pxf_batch_sync": (C.c_int, [vp]),
         "pxf_batch_destroy": (None, [vp]),
         "pxf_batch_last_error": (C.c_char_p, [vp]),
+        "pxf_batch_step_timed": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_double)]),
+        "pxf_server_config_init": (None, [C.POINTER(ServerConfig)]),
+        "pxf_server_create": (C.c_int, [C.POINTER(ServerConfig), pp]),
+        "pxf_server_submit": (C.c_int, [vp, dp, C.c_uint32, C.c_double, op, C.c_uint32, C.POINTER(C.c_uint64)]),
+        "pxf_server_cancel": (C.c_int, [vp, C.c_uint64]),
+        "pxf_server_tick": (C.c_int, [vp, u32p]),
+        "pxf_server_status": (C.c_int, [vp, C.c_uint64, C.POINTER(RequestStatus)]),
+        "pxf_server_take_result": (C.c_int, [vp, C.c_uint64, vp, C.c_size_t]),
+        "pxf_server_stats_get": (C.c_int, [vp, C.POINTER(ServerStats)]),
+        "pxf_server_start": (C.c_int, [vp]),
+        "pxf_server_stop": (C.c_int, [vp]),
+        "pxf_server_destroy": (None, [vp]),
+        "pxf_server_last_error": (C.c_char_p, [vp]),
     }
 
 

@@ -289,6 +289,10 @@ static cudaError_t end_capture_to_exec(cudaStream_t st, cudaGraphExec_t* exec) {
 int BatchImpl::capture() {
     const int n = int(sims.size());
     cudaError_t e;
+    // PXF_NO_COND_GRAPH=1 selects the host-driven precision loop (its graphs have no conditional
+    // node, which is what kernel profilers need to attribute the loop's kernels).
+    static const bool no_cond = [] { const char* v = std::getenv("PXF_NO_COND_GRAPH"); return v && v[0] == '1'; }();
+    if (no_cond) cond_ok = false;
     if (!any_pcg || cond_ok) {
         if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
             return cuda_fail(e, "begin capture");
@@ -1133,5 +1137,30 @@ void pxf_batch_destroy(pxf_batch* b) {
 }
 
 const char* pxf_batch_last_error(const pxf_batch* b) { return b ? b->impl.err.c_str() : g_last_error.c_str(); }
+
+int pxf_batch_step_timed(pxf_batch* b, uint32_t n, double* ms) {
+    if (!b || !ms) return set_global_error(PXF_EINVAL, "NULL argument");
+    BatchImpl& B = b->impl;
+    *ms = 0;
+    if (B.sims.empty() || n == 0) return PXF_OK;
+    if (B.dirty) {
+        int rc = B.rebuild();
+        if (rc) return rc;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, B.stream);
+    int rc = B.step(n);
+    cudaEventRecord(e1, B.stream);
+    if (!rc) rc = B.wait();
+    float t = 0;
+    if (!rc) cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    *ms = double(t);
+    return PXF_OK;
+}
 
 }  // extern "C"

@@ -46,7 +46,7 @@ def test_one_substep_bit_exact(lib, shape):
                     [P.FluidBlock([0.05, 0.02, 0.03], [0.6, 0.5, 0.5], [0.3, -0.2, 0.1])],
                     resolution=37, particles_per_cell=3, pressure_iterations=30)
     elif shape == "thin":  # one axis at the 4-cell minimum
-        f = P.Fluid("thin", [[0, 0, 0], [1, 0.05, 1]], [P.FluidBlock([0, 0, 0], [1, 0.05, 0.6])],
+        f = P.Fluid("thin", [[0, 0, 0], [1, 0.25, 1]], [P.FluidBlock([0, 0, 0], [1, 0.25, 0.6])],
                     resolution=16, particles_per_cell=1, pressure_iterations=10)
     else:
         f = P.Fluid("two", [[-0.5, 0, 0], [0.5, 0.6, 0.4]],
