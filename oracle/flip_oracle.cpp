@@ -60,9 +60,11 @@ template <class T> struct Sim {
     T h, dt, flip, inv_h;
     T origin[3], gravity[3];
     uint32_t iterations;
-    // Pressure mode: 0 = red-black Gauss-Seidel (reference), 1 = PCG with FP32 vectors, FP64
-    // dot products, FP64 solution and FP64 restart residuals, 2 = Jacobi-PCG entirely in FP64.
+    // Pressure mode: 0 = red-black Gauss-Seidel (reference), 1 = Jacobi-PCG with FP32 vectors,
+    // FP64 dot products, FP64 solution and FP64 restart residuals, 2 = Jacobi-PCG entirely in FP64,
+    // 3 = as 1 with a multigrid V-cycle preconditioner in FP32 (the CUDA precision solver).
     int pmode = 0;
+    uint32_t mg_coarse_iters = 16;   // symmetric red-black iterations on the coarsest level
     double rtol = 1e-6;
     uint32_t max_iter = 2000, restart = 50;
     uint32_t last_iters = 0;
@@ -304,6 +306,162 @@ template <class T> struct Sim {
         }
     }
 
+    // ------------------------------------------------------------------ multigrid preconditioner
+    // Geometric V-cycle on the cell grid. Level l+1 halves each axis (ceil); a coarse cell is AIR
+    // if any child is AIR, else FLUID if any child is FLUID, else SOLID (children outside the
+    // fine grid count as SOLID). Each level's operator is the same 7-point system as level 0
+    // built from its own types. Smoothing is red-black Gauss-Seidel (pre: red, black; post:
+    // black, red), restriction sums the children's residuals times 1/2 and prolongation injects
+    // the coarse correction into every child, so restriction = prolongation^T / 2 and the cycle
+    // is a symmetric operator. The coarsest level (<= 512 cells) runs mg_coarse_iters
+    // red-black iterations followed by as many black-red iterations from zero.
+    struct Level {
+        int nx = 0, ny = 0, nz = 0;
+        std::vector<uint8_t> type, fmask, cnt;
+        std::vector<float> r, z;
+        int64_t nc() const { return int64_t(nx) * ny * nz; }
+        int64_t off(int n) const {
+            const int64_t st[3] = {1, int64_t(nx), int64_t(nx) * ny};
+            return (n & 1) ? st[n >> 1] : -st[n >> 1];
+        }
+    };
+    std::vector<Level> mg;
+
+    static void level_info(Level& L) {
+        const int64_t C = L.nc();
+        L.fmask.assign(C, 0);
+        L.cnt.assign(C, 0);
+        for (int64_t id = 0; id < C; id++) {
+            if (L.type[id] != FLUID) continue;
+            int c[3] = {int(id % L.nx), int((id / L.nx) % L.ny), int(id / (int64_t(L.nx) * L.ny))};
+            const int n3[3] = {L.nx, L.ny, L.nz};
+            uint8_t m = 0, k = 0;
+            for (int n = 0; n < 6; n++) {
+                int q[3] = {c[0], c[1], c[2]};
+                q[n >> 1] += (n & 1) ? 1 : -1;
+                uint8_t t = SOLID;
+                if (q[0] >= 0 && q[1] >= 0 && q[2] >= 0 && q[0] < n3[0] && q[1] < n3[1] && q[2] < n3[2])
+                    t = L.type[q[0] + int64_t(L.nx) * (q[1] + int64_t(L.ny) * q[2])];
+                if (t == SOLID) continue;
+                k++;
+                if (t == FLUID) m |= uint8_t(1u << n);
+            }
+            L.fmask[id] = m;
+            L.cnt[id] = k;
+        }
+    }
+
+    void mg_build() {
+        mg.clear();
+        Level L0;
+        L0.nx = int(nx); L0.ny = int(ny); L0.nz = int(nz);
+        L0.type.resize(n_cells());
+        for (uint32_t i = 0; i < n_cells(); i++) L0.type[i] = uint8_t(cell_type[i]);
+        level_info(L0);
+        L0.r.assign(L0.nc(), 0.0f);
+        L0.z.assign(L0.nc(), 0.0f);
+        mg.push_back(std::move(L0));
+        while (mg.back().nc() > 512 && mg.back().nx >= 2 && mg.back().ny >= 2 && mg.back().nz >= 2) {
+            const Level& F = mg.back();
+            Level Cc;
+            Cc.nx = (F.nx + 1) / 2; Cc.ny = (F.ny + 1) / 2; Cc.nz = (F.nz + 1) / 2;
+            Cc.type.assign(Cc.nc(), SOLID);
+            for (int K = 0; K < Cc.nz; K++)
+                for (int J = 0; J < Cc.ny; J++)
+                    for (int I = 0; I < Cc.nx; I++) {
+                        bool air = false, fluid = false;
+                        for (int ch = 0; ch < 8; ch++) {
+                            int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), k = 2 * K + (ch >> 2);
+                            if (i >= F.nx || j >= F.ny || k >= F.nz) continue;
+                            uint8_t t = F.type[i + int64_t(F.nx) * (j + int64_t(F.ny) * k)];
+                            if (t == AIR) air = true;
+                            if (t == FLUID) fluid = true;
+                        }
+                        Cc.type[I + int64_t(Cc.nx) * (J + int64_t(Cc.ny) * K)] = air ? AIR : (fluid ? FLUID : SOLID);
+                    }
+            level_info(Cc);
+            Cc.r.assign(Cc.nc(), 0.0f);
+            Cc.z.assign(Cc.nc(), 0.0f);
+            mg.push_back(std::move(Cc));
+        }
+    }
+
+    static bool in_sys(const Level& L, int64_t id) { return L.type[id] == FLUID && L.cnt[id] > 0; }
+
+    // One red-black half sweep of A z = r on level L. first: the other colour is zero.
+    static void smooth(Level& L, int color, bool first) {
+        const int64_t C = L.nc();
+#pragma omp parallel for schedule(static)
+        for (int64_t id = 0; id < C; id++) {
+            if (!in_sys(L, id)) continue;
+            int i = int(id % L.nx), j = int((id / L.nx) % L.ny), k = int(id / (int64_t(L.nx) * L.ny));
+            if (((i + j + k) & 1) != color) continue;
+            float s = L.r[id];
+            if (!first) {
+                for (int n = 0; n < 6; n++)
+                    if (L.fmask[id] & (1u << n)) s += L.z[id + L.off(n)];
+            }
+            L.z[id] = s / float(L.cnt[id]);
+        }
+    }
+
+    static float resid(const Level& L, int64_t id) {
+        float az = float(L.cnt[id]) * L.z[id];
+        for (int n = 0; n < 6; n++)
+            if (L.fmask[id] & (1u << n)) az -= L.z[id + L.off(n)];
+        return L.r[id] - az;
+    }
+
+    void restrict_to(int l) {
+        const Level& F = mg[l];
+        Level& Cc = mg[l + 1];
+        const int64_t C = Cc.nc();
+#pragma omp parallel for schedule(static)
+        for (int64_t P = 0; P < C; P++) {
+            float s = 0.0f;
+            if (in_sys(Cc, P)) {
+                int I = int(P % Cc.nx), J = int((P / Cc.nx) % Cc.ny), K = int(P / (int64_t(Cc.nx) * Cc.ny));
+                for (int ch = 0; ch < 8; ch++) {
+                    int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), k = 2 * K + (ch >> 2);
+                    if (i >= F.nx || j >= F.ny || k >= F.nz) continue;
+                    int64_t id = i + int64_t(F.nx) * (j + int64_t(F.ny) * k);
+                    if (in_sys(F, id)) s += resid(F, id);
+                }
+            }
+            Cc.r[P] = 0.5f * s;
+        }
+    }
+
+    void prolong_from(int l) {
+        Level& F = mg[l];
+        const Level& Cc = mg[l + 1];
+        const int64_t C = F.nc();
+#pragma omp parallel for schedule(static)
+        for (int64_t id = 0; id < C; id++) {
+            if (!in_sys(F, id)) continue;
+            int i = int(id % F.nx), j = int((id / F.nx) % F.ny), k = int(id / (int64_t(F.nx) * F.ny));
+            int64_t P = (i >> 1) + int64_t(Cc.nx) * ((j >> 1) + int64_t(Cc.ny) * (k >> 1));
+            if (in_sys(Cc, P)) F.z[id] += Cc.z[P];
+        }
+    }
+
+    void vcycle(int l) {
+        Level& L = mg[l];
+        if (l + 1 == int(mg.size())) {
+            std::fill(L.z.begin(), L.z.end(), 0.0f);
+            for (uint32_t it = 0; it < mg_coarse_iters; it++) { smooth(L, 0, false); smooth(L, 1, false); }
+            for (uint32_t it = 0; it < mg_coarse_iters; it++) { smooth(L, 1, false); smooth(L, 0, false); }
+            return;
+        }
+        smooth(L, 0, true);
+        smooth(L, 1, false);
+        restrict_to(l);
+        vcycle(l + 1);
+        prolong_from(l);
+        smooth(L, 1, false);
+        smooth(L, 0, false);
+    }
+
     // Jacobi-preconditioned CG as a state machine shared by both PCG forms and mirrored by the
     // CUDA precision solver:
     //   restart: r = b - A x in FP64; converged if |r| <= rtol |b| (or iteration cap reached);
@@ -312,11 +470,11 @@ template <class T> struct Sim {
     //            restart when the recurrence |r| <= rtol |b|, every `restart` steps, or at the cap
     // V is the vector type of r, p, Ap (float for the precision form, double for the FP64 form);
     // x and every dot product are FP64.
-    template <class V> void pcg_run() {
+    template <class V> void pcg_run(bool use_mg) {
         Sys S; build_sys(S);
         const int64_t M = int64_t(S.idx.size());
         const uint32_t C = n_cells();
-        std::vector<V> r(M), p(M, V(0)), Ap(M), pg(C, V(0)), cnt(M);
+        std::vector<V> r(M), z(M), p(M, V(0)), Ap(M), pg(C, V(0)), cnt(M);
         std::vector<double> rd(M);
         for (int64_t k = 0; k < M; k++) cnt[k] = V(S.diag[k]);
         double bb = 0;
@@ -328,6 +486,26 @@ template <class T> struct Sim {
             finish_pcg(S);
             return;
         }
+        if (use_mg) mg_build();
+        // z = M^-1 r
+        auto precond = [&]() {
+            if (!use_mg) {
+#pragma omp parallel for schedule(static)
+                for (int64_t k = 0; k < M; k++) z[k] = r[k] / cnt[k];
+                return;
+            }
+            Level& L0 = mg[0];
+            std::fill(L0.r.begin(), L0.r.end(), 0.0f);
+            for (int64_t k = 0; k < M; k++) L0.r[S.idx[k]] = float(r[k]);
+            vcycle(0);
+            for (int64_t k = 0; k < M; k++) z[k] = V(L0.z[S.idx[k]]);
+        };
+        auto dot_rz = [&]() {
+            double t = 0;
+#pragma omp parallel for schedule(static) reduction(+ : t)
+            for (int64_t k = 0; k < M; k++) t += double(r[k]) * double(z[k]);
+            return t;
+        };
         const double tol2 = rtol * rtol * bb;
         uint32_t it = 0, since = 0;
         double rz = 0, beta = 0;
@@ -339,10 +517,8 @@ template <class T> struct Sim {
             for (int64_t k = 0; k < M; k++) { rd[k] = S.b[k] - rd[k]; rr += rd[k] * rd[k]; r[k] = V(rd[k]); }
             last_relres = std::sqrt(rr / bb);
             if (rr <= tol2 || it >= max_iter) { done = true; return; }
-            double rzl = 0;
-#pragma omp parallel for schedule(static) reduction(+ : rzl)
-            for (int64_t k = 0; k < M; k++) { V z = r[k] / cnt[k]; rzl += double(r[k]) * double(z); }
-            rz = rzl;
+            precond();
+            rz = dot_rz();
             fresh = true; since = 0;
         };
         do_restart();
@@ -351,8 +527,7 @@ template <class T> struct Sim {
             const bool fr = fresh;
 #pragma omp parallel for schedule(static)
             for (int64_t k = 0; k < M; k++) {
-                V z = r[k] / cnt[k];
-                p[k] = fr ? z : V(z + bv * p[k]);
+                p[k] = fr ? z[k] : V(z[k] + bv * p[k]);
                 pg[S.idx[k]] = p[k];
             }
             fresh = false;
@@ -369,19 +544,19 @@ template <class T> struct Sim {
             if (!(pAp > 0)) break;   // breakdown (non-SPD or NaN): stop with the current x
             const double alpha = rz / pAp;
             const V av = V(alpha);
-            double rr = 0, rzn = 0;
-#pragma omp parallel for schedule(static) reduction(+ : rr, rzn)
+            double rr = 0;
+#pragma omp parallel for schedule(static) reduction(+ : rr)
             for (int64_t k = 0; k < M; k++) {
                 xp64[S.idx[k]] += alpha * double(p[k]);
                 r[k] = r[k] - av * Ap[k];
-                V z = r[k] / cnt[k];
                 rr += double(r[k]) * double(r[k]);
-                rzn += double(r[k]) * double(z);
             }
             it++; since++;
             if (rr <= tol2 || since >= restart || it >= max_iter) {
                 do_restart();
             } else {
+                precond();
+                const double rzn = dot_rz();
                 beta = rzn / rz;
                 rz = rzn;
             }
@@ -389,8 +564,9 @@ template <class T> struct Sim {
         last_iters = it;
         finish_pcg(S);
     }
-    void pcg_mixed() { pcg_run<float>(); }
-    void pcg_fp64() { pcg_run<double>(); }
+    void pcg_mixed() { pcg_run<float>(false); }
+    void pcg_fp64() { pcg_run<double>(false); }
+    void pcg_mg() { pcg_run<float>(true); }
     void finish_pcg(const Sys&) {
         const int64_t C = n_cells();
 #pragma omp parallel for schedule(static)
@@ -460,6 +636,8 @@ template <class T> struct Sim {
                 for (uint32_t parity = 0; parity < 2; parity++) pressure_rb(parity);
         } else if (pmode == 1) {
             pcg_mixed();
+        } else if (pmode == 3) {
+            pcg_mg();
         } else {
             pcg_fp64();
         }

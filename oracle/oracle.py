@@ -122,7 +122,7 @@ class OracleSim:
             self.h = None
 
     def set_pressure(self, mode, rtol=1e-6, max_iter=2000, restart=50):
-        modes = {"gs": 0, "pcg": 1, "pcg64": 2}
+        modes = {"gs": 0, "pcg": 1, "pcg64": 2, "mgpcg": 3}
         self.lib.orc_sim_set_pressure(self.h, modes.get(mode, mode), rtol, max_iter, restart)
 
     def pcg_stats(self):
