@@ -103,6 +103,7 @@ def _sig():
         "pxf_set_device": (C.c_int, [C.c_int]),
         "pxf_host_alloc": (C.c_int, [C.c_size_t, pp]),
         "pxf_host_free": (None, [vp]),
+        "pxf_cell_starts_noalloc": (C.c_int, [vp, C.c_uint32, u32p, C.POINTER(C.c_float), C.c_float, vp, vp]),
         "pxf_destroy": (None, [vp]),
         "pxf_last_error": (C.c_char_p, [vp]),
         "pxf_batch_create": (C.c_int, [pp]),

@@ -513,6 +513,8 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
     return PXF_OK;
 }
 
+void set_global_error_message(const std::string& m) { g_last_error = m; }
+
 int p2g_shape_index() {
     static int shape = -2;
     if (shape == -2) {
