@@ -70,7 +70,8 @@ typedef struct {
 } pxf_fluid_desc;
 
 #define PXF_PRESSURE_RBGS 0u   /* red-black Gauss-Seidel, pressure_iterations sweeps (reference) */
-#define PXF_PRESSURE_PCG 1u    /* Jacobi PCG: FP32 vectors, FP64 dots, FP64 solution + restarts */
+#define PXF_PRESSURE_PCG 1u    /* PCG (multigrid or Jacobi preconditioner): FP32 vectors, double-float
+                                  solution, FP64 reductions and FP64 restart residuals */
 
 /* Options beyond the reference's Fluid block. pxf_options_init gives the reference behaviour. */
 typedef struct {
@@ -84,6 +85,8 @@ typedef struct {
     uint32_t velocity_seed;        /* seed of that jitter */
     double wait_timeout_s;         /* bound on every host wait, default 600 s */
     int32_t p2g_tile;              /* P2G tile shape index (-1: tuned / default) */
+    uint32_t pcg_precond;          /* 0: multigrid V-cycle (default), 1: Jacobi */
+    uint32_t mg_coarse_iters;      /* red-black iterations on the coarsest multigrid level, default 16 */
 } pxf_options;
 
 PXF_API void pxf_fluid_desc_init(pxf_fluid_desc* desc);

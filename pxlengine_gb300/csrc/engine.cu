@@ -54,6 +54,7 @@ struct BatchImpl {
     uint32_t* d_base = nullptr;
     size_t cap_sims = 0;
     StageWork w_parts, w_tiles, w_cells, w_half, w_faces, w_chunks;
+    PcgWork pw;                          // precision-solver work indexes
     uint32_t max_gs_iters = 0;
     bool any_gs = false, any_pcg = false;
     int tile_shape = 0;
@@ -115,6 +116,7 @@ struct pxf_snapshot {
     std::vector<float4> pos, vel;
     std::vector<float> pressure;
     std::vector<double> x64;
+    std::vector<float2> x2;
     uint64_t steps_done = 0;
     bool initialized = false;
     uint32_t np = 0, nc = 0;
@@ -129,8 +131,26 @@ namespace pxf {
 // Byte layout of one simulation's allocation.
 struct Layout {
     size_t posA, velA, posB, velB, pos0, vel0, vel, vel_old, pressure, div, type, count, start, chunk, info, acc, wacc,
-        x64, r, p0, p1, Ap, partial, pcg, total;
+        x2, x64, r, z, p0, p1, Ap, partial, pcg, total;
+    int nlev = 0;
+    int dims[kMaxLevels][3];
+    size_t ltype[kMaxLevels], linfo[kMaxLevels], lr[kMaxLevels], lz[kMaxLevels];
 };
+
+// Multigrid hierarchy: halve (rounding up) while the level has more than 512 cells and every
+// axis has at least 2 cells.
+static int mg_levels(const uint32_t n[3], int dims[kMaxLevels][3]) {
+    int L = 0;
+    dims[0][0] = int(n[0]); dims[0][1] = int(n[1]); dims[0][2] = int(n[2]);
+    L = 1;
+    while (L < kMaxLevels) {
+        const int* d = dims[L - 1];
+        if (int64_t(d[0]) * d[1] * d[2] <= 512 || d[0] < 2 || d[1] < 2 || d[2] < 2) break;
+        for (int a = 0; a < 3; a++) dims[L][a] = (d[a] + 1) / 2;
+        L++;
+    }
+    return L;
+}
 
 static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o) {
     const uint64_t nc = uint64_t(n[0]) * n[1] * n[2];
@@ -159,13 +179,27 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
     L.acc = o.keep_p2g_sums ? take(4 * nf) : 0;
     L.wacc = o.keep_p2g_sums ? take(4 * nf) : 0;
     const bool pcg = o.pressure_solver == PXF_PRESSURE_PCG;
-    L.x64 = pcg ? take(8 * nc) : 0;
-    L.r = pcg ? take(4 * nc) : 0;
-    L.p0 = pcg ? take(4 * nc) : 0;
-    L.p1 = pcg ? take(4 * nc) : 0;
-    L.Ap = pcg ? take(4 * nc) : 0;
-    L.partial = pcg ? take(16 * nchunks) : 0;
-    L.pcg = pcg ? take(sizeof(PcgState)) : 0;
+    if (pcg) {
+        L.x2 = take(8 * nc);
+        L.x64 = take(8 * nc);
+        L.r = take(4 * nc);
+        L.z = take(4 * nc);
+        L.p0 = take(4 * nc);
+        L.p1 = take(4 * nc);
+        L.Ap = take(4 * nc);
+        L.partial = take(8 * nchunks);
+        L.pcg = take(sizeof(PcgState));
+        if (o.pcg_precond == 0) {
+            L.nlev = mg_levels(n, L.dims);
+            for (int l = 1; l < L.nlev; l++) {
+                const uint64_t c = uint64_t(L.dims[l][0]) * L.dims[l][1] * L.dims[l][2];
+                L.ltype[l] = take(c);
+                L.linfo[l] = take(2 * c);
+                L.lr[l] = take(4 * c);
+                L.lz[l] = take(4 * c);
+            }
+        }
+    }
     L.total = off;
     return L;
 }
@@ -190,6 +224,10 @@ void BatchImpl::drop_graphs() {
 
 static inline uint32_t cdiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1) / b); }
 
+// Work-index stages: particles, P2G tiles, cells, half cells, faces, 2048-cell chunks, then the
+// multigrid smoothing chunks of each level and the restriction chunks of each level.
+constexpr int kStages = 6 + 2 * kMaxLevels;
+
 int BatchImpl::rebuild() {
     cudaError_t e;
     if (!stream) {
@@ -206,7 +244,7 @@ int BatchImpl::rebuild() {
         d_base = nullptr;
         cap_sims = std::max<size_t>(size_t(n), cap_sims * 2);
         if ((e = cudaMalloc(&d_sims, cap_sims * sizeof(SimDev))) != cudaSuccess) return cuda_fail(e, "batch table");
-        if ((e = cudaMalloc(&d_base, 6 * (cap_sims + 1) * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "batch index");
+        if ((e = cudaMalloc(&d_base, kStages * (cap_sims + 1) * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "batch index");
     }
     tile_shape = p2g_shape_index();
     for (pxf_sim* sm : sims)
@@ -214,24 +252,38 @@ int BatchImpl::rebuild() {
     int shape[3];
     p2g_shape(tile_shape, shape);
     std::vector<SimDev> host(n);
-    std::vector<uint32_t> base(6 * (n + 1), 0);
+    std::vector<uint32_t> base(kStages * (n + 1), 0);
     max_gs_iters = 0;
     any_gs = any_pcg = false;
+    pw = PcgWork();
     timeout_s = 0;
     for (int i = 0; i < n; i++) {
         pxf_sim* s = sims[i];
         host[i] = s->dev;
         const SimDev& d = s->dev;
-        const uint32_t items[6] = {
+        uint32_t items[kStages] = {
             cdiv(d.np, kElemItem),
             cdiv(d.nx, shape[0]) * cdiv(d.ny, shape[1]) * cdiv(d.nz, shape[2]),
             cdiv(d.nc, kElemItem),
             cdiv(uint64_t((d.nx + 1) / 2) * d.ny * d.nz, kElemItem),
             cdiv(d.nf, kElemItem),
             cdiv(d.nc, kScanChunk)};
-        for (int k = 0; k < 6; k++) base[k * (n + 1) + i + 1] = base[k * (n + 1) + i] + items[k];
-        if (d.solver == 0) { any_gs = true; max_gs_iters = std::max(max_gs_iters, d.iterations); }
-        else any_pcg = true;
+        const bool mg = d.solver == 1 && d.precond == 0;
+        for (int l = 0; l < kMaxLevels; l++) {
+            // level l smoothing and restriction to l + 1 exist when level l is not the coarsest
+            const bool has = mg && l + 1 < d.nlev;
+            items[6 + l] = has ? cdiv(d.lev[l].nc, kScanChunk) : 0;
+            items[6 + kMaxLevels + l] = has ? cdiv(d.lev[l + 1].nc, kScanChunk) : 0;
+        }
+        for (int k = 0; k < kStages; k++) base[k * (n + 1) + i + 1] = base[k * (n + 1) + i] + items[k];
+        if (d.solver == 0) {
+            any_gs = true;
+            max_gs_iters = std::max(max_gs_iters, d.iterations);
+        } else {
+            any_pcg = true;
+            if (mg) { pw.any_mg = true; pw.max_levels = std::max(pw.max_levels, d.nlev); }
+            else pw.any_jacobi = true;
+        }
         timeout_s = std::max(timeout_s, s->opts.wait_timeout_s);
     }
     if (timeout_s <= 0) timeout_s = 600.0;
@@ -240,13 +292,21 @@ int BatchImpl::rebuild() {
     if ((e = cudaMemcpyAsync(d_base, base.data(), base.size() * 4, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
         return cuda_fail(e, "batch index upload");
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "batch upload");
-    StageWork* ws[6] = {&w_parts, &w_tiles, &w_cells, &w_half, &w_faces, &w_chunks};
-    for (int k = 0; k < 6; k++) {
+    StageWork* ws[kStages];
+    ws[0] = &w_parts; ws[1] = &w_tiles; ws[2] = &w_cells; ws[3] = &w_half; ws[4] = &w_faces; ws[5] = &w_chunks;
+    for (int l = 0; l < kMaxLevels; l++) {
+        ws[6 + l] = &pw.level[l];
+        ws[6 + kMaxLevels + l] = &pw.coarse[l];
+    }
+    for (int k = 0; k < kStages; k++) {
         ws[k]->sims = d_sims;
         ws[k]->base = d_base + k * (n + 1);
         ws[k]->n_sims = n;
         ws[k]->total = base[k * (n + 1) + n];
     }
+    pw.sims = d_sims;
+    pw.n_sims = n;
+    pw.chunks = w_chunks;
     int rc = capture();
     if (rc) return rc;
     dirty = false;
@@ -265,13 +325,13 @@ int BatchImpl::record_pre(cudaStream_t st) {
             for (uint32_t parity = 0; parity < 2; parity++)
                 if ((e = launch_pressure_rb(w_half, parity, it, st)) != cudaSuccess) return cuda_fail(e, "pressure");
     }
-    if (any_pcg && (e = launch_pcg_init(w_chunks, st)) != cudaSuccess) return cuda_fail(e, "pcg init");
+    if (any_pcg && (e = launch_pcg_init(pw, st)) != cudaSuccess) return cuda_fail(e, "pcg init");
     return PXF_OK;
 }
 
 int BatchImpl::record_post(cudaStream_t st) {
     cudaError_t e;
-    if (any_pcg && (e = launch_pcg_finish(w_chunks, st)) != cudaSuccess) return cuda_fail(e, "pcg finish");
+    if (any_pcg && (e = launch_pcg_finish(pw, st)) != cudaSuccess) return cuda_fail(e, "pcg finish");
     if ((e = launch_project(w_faces, st)) != cudaSuccess) return cuda_fail(e, "project");
     if ((e = launch_g2p(w_parts, st)) != cudaSuccess) return cuda_fail(e, "g2p");
     return PXF_OK;
@@ -326,7 +386,7 @@ int BatchImpl::capture() {
                 cudaGraph_t body = np.conditional.phGraph_out[0];
                 e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
-                    cudaError_t e1 = launch_pcg_body(w_chunks, side);
+                    cudaError_t e1 = launch_pcg_body(pw, side);
                     cudaError_t e2 = launch_pcg_cond(d_sims, n, h, side);
                     cudaGraph_t out = body;
                     cudaError_t e3 = cudaStreamEndCapture(side, &out);
@@ -358,7 +418,7 @@ int BatchImpl::capture() {
     if ((e = end_capture_to_exec(stream, &exec_pre)) != cudaSuccess && !rc) return cuda_fail(e, "graph pre");
     if (rc) return rc;
     if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cuda_fail(e, "capture");
-    for (int k = 0; k < 8; k++) launch_pcg_body(w_chunks, stream);
+    for (int k = 0; k < 8; k++) launch_pcg_body(pw, stream);
     launch_pcg_any(d_sims, n, d_flag, stream);
     cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
     if ((e = end_capture_to_exec(stream, &exec_body)) != cudaSuccess) return cuda_fail(e, "graph body");
@@ -468,27 +528,26 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
             if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
             if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
         }
-        if ((e = launch_pcg_init(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
-        size_t t = ev(); add("pcg_init+restart", prev, t); prev = t;
+        if ((e = launch_pcg_init(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
+        size_t t = ev(); add("pcg_setup+init", prev, t); prev = t;
         for (uint32_t guard = 0; guard < 100000; guard++) {
-            if ((e = launch_pcg_dir_spmv(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t a = ev(); add("pcg_dir_spmv", prev, a);
-            if ((e = launch_pcg_update(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t b = ev(); add("pcg_update", a, b);
-            if ((e = launch_pcg_restart(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t c = ev(); add("pcg_restart", b, c);
-            prev = c;
-            if ((guard & 7) == 7) {
-                launch_pcg_any(d_sims, n, d_flag, stream);
-                cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
-                int rc = wait();
-                if (rc) return rc;
-                size_t d = ev();
-                prev = d;
-                if (*h_flag == 0) break;
-            }
+            if ((e = launch_pcg_dir(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t a1 = ev(); add("pcg_dir", prev, a1);
+            if ((e = launch_pcg_update(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t b1 = ev(); add("pcg_update", a1, b1);
+            if ((e = launch_pcg_restart(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t c1 = ev(); add("pcg_restart_check", b1, c1);
+            if ((e = launch_precond(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            size_t d1 = ev(); add(pw.any_mg ? "mg_vcycle" : "jacobi", c1, d1);
+            prev = d1;
+            launch_pcg_any(d_sims, n, d_flag, stream);
+            cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
+            int rc = wait();
+            if (rc) return rc;
+            prev = ev();
+            if (*h_flag == 0) break;
         }
-        if ((e = launch_pcg_finish(w_chunks, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
+        if ((e = launch_pcg_finish(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
         size_t f = ev(); add("pcg_finish", prev, f); prev = f;
     }
     if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
@@ -581,6 +640,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     if (!validate_fluid(cfg, 0, opts.lift_grid_limits != 0, msg)) return set_global_error(PXF_EINVAL, msg);
     if (!(fps > 0.0)) return set_global_error(PXF_EINVAL, "render.fps must be > 0");
     if (opts.pressure_solver > PXF_PRESSURE_PCG) return set_global_error(PXF_EINVAL, "unknown pressure_solver");
+    if (opts.pcg_precond > 1) return set_global_error(PXF_EINVAL, "unknown pcg_precond");
     if (ensure_device(msg)) return set_global_error(PXF_ECUDA, msg);
 
     std::unique_ptr<pxf_sim> s(new pxf_sim());
@@ -620,6 +680,8 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.rtol = opts.pcg_rtol;
     d.max_iter = opts.pcg_max_iter;
     d.restart = opts.pcg_restart ? opts.pcg_restart : 50;
+    d.precond = opts.pcg_precond;
+    d.coarse_iters = opts.mg_coarse_iters ? opts.mg_coarse_iters : 16;
 
     cudaError_t e = cudaMalloc(&s->mem, L.total);
     if (e != cudaSuccess) {
@@ -647,13 +709,31 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.acc = opts.keep_p2g_sums ? reinterpret_cast<int32_t*>(m + L.acc) : nullptr;
     d.wacc = opts.keep_p2g_sums ? reinterpret_cast<int32_t*>(m + L.wacc) : nullptr;
     if (opts.pressure_solver == PXF_PRESSURE_PCG) {
+        d.x2 = reinterpret_cast<float2*>(m + L.x2);
         d.x64 = reinterpret_cast<double*>(m + L.x64);
         d.r = reinterpret_cast<float*>(m + L.r);
+        d.z = reinterpret_cast<float*>(m + L.z);
         d.p0 = reinterpret_cast<float*>(m + L.p0);
         d.p1 = reinterpret_cast<float*>(m + L.p1);
         d.Ap = reinterpret_cast<float*>(m + L.Ap);
         d.partial = reinterpret_cast<double*>(m + L.partial);
         d.pcg = reinterpret_cast<PcgState*>(m + L.pcg);
+        d.nlev = L.nlev > 0 ? L.nlev : 1;
+        d.lev[0].nx = d.nx; d.lev[0].ny = d.ny; d.lev[0].nz = d.nz;
+        d.lev[0].nc = d.nc;
+        d.lev[0].type = d.type;
+        d.lev[0].info = d.info;
+        d.lev[0].r = d.r;
+        d.lev[0].z = d.z;
+        for (int l = 1; l < L.nlev; l++) {
+            MgLevel& v = d.lev[l];
+            v.nx = L.dims[l][0]; v.ny = L.dims[l][1]; v.nz = L.dims[l][2];
+            v.nc = uint32_t(v.nx) * uint32_t(v.ny) * uint32_t(v.nz);
+            v.type = reinterpret_cast<uint8_t*>(m + L.ltype[l]);
+            v.info = reinterpret_cast<uint16_t*>(m + L.linfo[l]);
+            v.r = reinterpret_cast<float*>(m + L.lr[l]);
+            v.z = reinterpret_cast<float*>(m + L.lz[l]);
+        }
     }
 
     s->own = new BatchImpl();
@@ -718,6 +798,8 @@ void pxf_options_init(pxf_options* o) {
     o->pcg_restart = 50;
     o->wait_timeout_s = 600.0;
     o->p2g_tile = -1;
+    o->pcg_precond = 0;
+    o->mg_coarse_iters = 16;
 }
 
 int pxf_validate(const pxf_fluid_desc* desc, uint32_t index, uint32_t lift, char* msg, size_t cap) {
@@ -939,8 +1021,13 @@ int pxf_write_grid(pxf_sim* s, int which, const void* in, size_t bytes) {
     if (e == cudaSuccess && d.x64) {
         const float* p = static_cast<const float*>(in);
         std::vector<double> x(d.nc);
-        for (uint32_t i = 0; i < d.nc; i++) x[i] = double(p[i]);
+        std::vector<float2> x2(d.nc);
+        for (uint32_t i = 0; i < d.nc; i++) {
+            x[i] = double(p[i]);
+            x2[i] = make_float2(p[i], 0.0f);
+        }
         e = cudaMemcpyAsync(d.x64, x.data(), 8ull * d.nc, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d.x2, x2.data(), 8ull * d.nc, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
     if (e != cudaSuccess) return s->cuda_fail(e, "write grid");
@@ -977,7 +1064,9 @@ int pxf_snapshot_take(pxf_sim* s, pxf_snapshot** out) {
     if (e == cudaSuccess) e = cudaMemcpy(snap->pressure.data(), d.pressure, 4ull * d.nc, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && d.x64) {
         snap->x64.resize(d.nc);
+        snap->x2.resize(d.nc);
         e = cudaMemcpy(snap->x64.data(), d.x64, 8ull * d.nc, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(snap->x2.data(), d.x2, 8ull * d.nc, cudaMemcpyDeviceToHost);
     }
     if (e != cudaSuccess) return s->cuda_fail(e, "snapshot");
     snap->steps_done = s->steps_done;
@@ -998,6 +1087,8 @@ int pxf_snapshot_restore(pxf_sim* s, const pxf_snapshot* snap) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(d.pressure, snap->pressure.data(), 4ull * d.nc, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && d.x64 && snap->x64.size() == d.nc)
         e = cudaMemcpyAsync(d.x64, snap->x64.data(), 8ull * d.nc, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && d.x2 && snap->x2.size() == d.nc)
+        e = cudaMemcpyAsync(d.x2, snap->x2.data(), 8ull * d.nc, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return s->cuda_fail(e, "restore");
     rc = sim_bin(s, st);
     if (rc) return rc;

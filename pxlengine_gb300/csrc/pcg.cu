@@ -1,17 +1,31 @@
-// Precision pressure solve: Jacobi-preconditioned CG with FP32 vectors (r, p, Ap), an FP64
-// solution x and FP64 dot products / restart residuals. It solves the system that
-// shaders/fluid.slang:167-182 relaxes: for each fluid cell i,
-//     cnt_i p_i - sum_{fluid j} p_j = -(div_i h h / dt),     cnt_i = non-solid neighbours.
+// Precision pressure solve: preconditioned CG on the system that shaders/fluid.slang:167-182
+// relaxes, for each fluid cell i
+//     cnt_i p_i - sum_{fluid j} p_j = -(div_i h h / dt),     cnt_i = non-solid neighbours,
+// with a geometric multigrid V-cycle (or Jacobi) preconditioner.
 //
-// Per step, two passes over the cells plus a conditional third:
-//   k_pcg_dir_spmv  p' = z + beta p (z = r / cnt, recomputed for the 6 neighbours on the fly),
-//                   Ap = A p', partial p'.Ap                 -> alpha
-//   k_pcg_update    x += alpha p', r -= alpha Ap, partial r.r and r.z
-//                                                              -> beta, or a restart request
-//   k_pcg_restart   r = b - A x in FP64 for simulations that asked for it -> converged / fresh
-// Every reduction is per simulation: fixed-order block reductions into per-chunk partials, and
-// the last block of a simulation sums those partials in chunk order. Results therefore do not
-// depend on scheduling or on which other simulations share the launch.
+// Precision: vectors r, z, p, Ap and the whole V-cycle are FP32. The solution x is kept as a
+// double-float pair (hi + lo, 48-bit significand) so the true residual can fall below FP32's
+// cond(A)·eps floor. The FP64 steps are the reductions and the restart residual:
+//   * dot products: each product is formed exactly (FP32 two-product), a warp sums its products
+//     in double-float, and warp / block / chunk sums are FP64 in a fixed order;
+//   * restart: x is widened to FP64 and r = b - A x is evaluated in FP64 (every `restart` steps,
+//     when the recurrence residual reaches the target, and at the iteration cap); convergence is
+//     declared on that FP64 residual, |r| <= rtol |b|.
+// (GB300's FP64 pipe runs at about 1 TFLOP/s, 1/60 of FP32, so FP64 is kept out of per-cell work.)
+//
+// Reductions never use atomics or fences: every 2048-cell chunk writes its partial sums, and a
+// one-block control kernel per simulation sums them in chunk order and advances that simulation's
+// solver state. Results therefore do not depend on scheduling or on the other simulations of a
+// batch.
+//
+// Multigrid (level l+1 halves each axis, rounding up): a coarse cell is AIR if any child is AIR,
+// else FLUID if any child is FLUID, else SOLID (children outside the fine grid are SOLID); each
+// level's operator is the 7-point system above built from its own types. V-cycle: red-black
+// Gauss-Seidel pre-smoothing (red from zero, black), restriction r_c = 1/2 * sum of the children's
+// residuals, recursion, prolongation (each child += its parent's correction, fused into the first
+// post-smoothing sweep), post-smoothing (black, red). The coarsest level (<= 512 cells) runs
+// `coarse_iters` red-black then as many black-red iterations from zero in one block. Restriction
+// is prolongation^T / 2 and the sweeps mirror each other, so the cycle is symmetric.
 #include "pxf_device.cuh"
 #include "pxf_kernels.h"
 
@@ -20,60 +34,48 @@ namespace pxf {
 namespace {
 
 constexpr int THREADS = 256;
-constexpr int PER_THREAD = kScanChunk / THREADS;   // 8 cells per thread
+constexpr int PER_THREAD = kScanChunk / THREADS;   // 8 cells per thread, strided by 256
 
-// Block-wide sums of two doubles in a fixed order. Result valid in thread 0.
-__device__ __forceinline__ void block_sum2(double& a, double& b, double* sh) {
+// ---------------------------------------------------------------- double-float arithmetic
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF two_prod(float a, float b) {
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    const float s = a.hi + b.hi;
+    const float bv = s - a.hi;
+    float e = (a.hi - (s - bv)) + (b.hi - bv);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    return {hi, e - (hi - s)};
+}
+
+// Block sum of a double-float accumulator in a fixed order; valid in thread 0.
+__device__ __forceinline__ double block_sum(DF a, double* sh) {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, d);
-        b += __shfl_down_sync(0xffffffffu, b, d);
+        const DF t{__shfl_down_sync(0xffffffffu, a.hi, d), __shfl_down_sync(0xffffffffu, a.lo, d)};
+        a = df_add(a, t);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { sh[2 * wid] = a; sh[2 * wid + 1] = b; }
+    if (lane == 0) sh[wid] = double(a.hi) + double(a.lo);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        a = 0; b = 0;
-        for (int k = 0; k < THREADS / 32; k++) { a += sh[2 * k]; b += sh[2 * k + 1]; }
-    }
+    double out = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < THREADS / 32; k++) out += sh[k];
     __syncthreads();
-}
-
-// Writes this chunk's partials; returns true (in every thread) for the last chunk of the
-// simulation to arrive, after which that block may read all partials of the simulation.
-__device__ __forceinline__ bool arrive_last(const SimDev& s, uint32_t chunk, uint32_t nchunks, double a, double b,
-                                            uint32_t* counter, bool* flag) {
-    if (threadIdx.x == 0) {
-        s.partial[2 * chunk] = a;
-        s.partial[2 * chunk + 1] = b;
-        __threadfence();
-        const uint32_t prev = atomicAdd(counter, 1u);
-        *flag = (prev == nchunks - 1);
-    }
-    __syncthreads();
-    const bool last = *flag;
-    if (last) __threadfence();
-    return last;
-}
-
-// Fixed-order sum of the per-chunk partials (last block only). Result valid in thread 0.
-__device__ __forceinline__ void sum_partials(const SimDev& s, uint32_t nchunks, double& a, double& b, double* sh) {
-    a = 0; b = 0;
-    for (uint32_t k = threadIdx.x; k < nchunks; k += THREADS) {
-        a += __ldcg(s.partial + 2 * k);
-        b += __ldcg(s.partial + 2 * k + 1);
-    }
-    block_sum2(a, b, sh);
-}
-
-__device__ __forceinline__ float rhs_of(const SimDev& s, uint32_t c) {
-    return s.div[c] * s.h * s.h / s.dt;   // fluid.slang:181
+    return out;
 }
 
 __device__ __forceinline__ bool in_system(uint32_t inf) { return (inf & 0x8000u) && ((inf >> 8) & 7u); }
+__device__ __forceinline__ float cnt_of(uint32_t inf) { return float((inf >> 8) & 7u); }
 
-__device__ __forceinline__ int64_t nbr_off(const SimDev& s, int q) {
-    const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
+__device__ __forceinline__ int64_t nbr(int q, int64_t nx, int64_t nxy) {
     switch (q) {
         case 0: return -1;
         case 1: return 1;
@@ -84,238 +86,482 @@ __device__ __forceinline__ int64_t nbr_off(const SimDev& s, int q) {
     }
 }
 
-// Scalars of the precision solver live in device memory written by the previous launch's last
-// block; read them through L2.
-__device__ __forceinline__ uint32_t ld_u32(const uint32_t* p) { return __ldcg(p); }
-__device__ __forceinline__ double ld_f64(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float rhs_of(const SimDev& s, uint32_t c) {
+    return s.div[c] * s.h * s.h / s.dt;   // fluid.slang:181
+}
+
+// Per-simulation scalars, written by the previous launch's control kernel: read through L2.
+__device__ __forceinline__ uint32_t ldu(const uint32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ double ldd(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ldf(const float* p) { return __ldcg(p); }
+
+__device__ __forceinline__ bool active(const SimDev& s) { return s.solver == 1 && !ldu(&s.pcg->done); }
+
+__device__ __forceinline__ uint32_t nchunks0(const SimDev& s) { return (s.nc + kScanChunk - 1) / kScanChunk; }
+
+// Fixed-order sum of a simulation's chunk partials (control kernels, one block per simulation).
+__device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
+    const uint32_t n = nchunks0(s);
+    double p = 0;
+    for (uint32_t k = threadIdx.x; k < n; k += THREADS) p += __ldcg(s.partial + k);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) p += __shfl_down_sync(0xffffffffu, p, d);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = p;
+    __syncthreads();
+    double out = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < THREADS / 32; k++) out += sh[k];
+    __syncthreads();
+    return out;
+}
 
 }  // namespace
 
-// -------------------------------------------------------------------------- init
-__global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) {
-    __shared__ double sh[16];
-    __shared__ bool last;
+// ============================================================================ multigrid setup
+// Type of level l+1 from its children on level l.
+__global__ void __launch_bounds__(THREADS) k_mg_coarsen(Work w, int l) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
-        const SimDev s = w.sims[si];
-        if (s.solver != 1) continue;
-        const uint32_t chunk = item - w.base[si];
-        const uint32_t nchunks = (s.nc + kScanChunk - 1) / kScanChunk;
-        double bb = 0, unused = 0;
-#pragma unroll
+        const SimDev* sp = w.sims + si;
+        if (sp->solver != 1) continue;
+        const MgLevel F = sp->lev[l], Cc = sp->lev[l + 1];
         for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c < s.nc && in_system(s.info[c])) {
-                const double b = -double(rhs_of(s, c));
-                bb += b * b;
+            const uint32_t P = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+            if (P >= Cc.nc) continue;
+            const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
+            const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
+            bool air = false, fluid = false;
+#pragma unroll
+            for (int ch = 0; ch < 8; ch++) {
+                const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
+                if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
+                const uint8_t t = F.type[uint32_t(i) + uint32_t(F.nx) * (uint32_t(j) + uint32_t(F.ny) * uint32_t(kk))];
+                air |= (t == AIR);
+                fluid |= (t == FLUID);
             }
-        }
-        block_sum2(bb, unused, sh);
-        PcgState* st = s.pcg;
-        if (arrive_last(s, chunk, nchunks, bb, 0.0, &st->arrive, &last)) {
-            sum_partials(s, nchunks, bb, unused, sh);
-            if (threadIdx.x == 0) {
-                st->bb = bb;
-                st->iters = 0;
-                st->since = 0;
-                st->fresh = 1;
-                st->status = 0;
-                st->relres = 0;
-                st->beta = 0;
-                st->restart_now = 1;
-                st->done = 0;
-                st->zero_x = bb == 0.0 ? 1u : 0u;
-                st->arrive = 0;
-            }
+            Cc.type[P] = air ? AIR : (fluid ? FLUID : SOLID);
         }
     }
 }
 
-// -------------------------------------------------------------------------- restart
-// r = b - A x in FP64 for simulations that requested a restart (and the zero-rhs case).
-__global__ void __launch_bounds__(THREADS) k_pcg_restart(Work w) {
-    __shared__ double sh[16];
-    __shared__ bool last;
+// Neighbour record of level l+1 (as k_divergence builds it for level 0).
+__global__ void __launch_bounds__(THREADS) k_mg_info(Work w, int l) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
-        const SimDev s = w.sims[si];
-        if (s.solver != 1) continue;
-        PcgState* st = s.pcg;
-        if (ld_u32(&st->done) || !ld_u32(&st->restart_now)) continue;
-        const bool zero_x = ld_u32(&st->zero_x) != 0;
-        const uint32_t chunk = item - w.base[si];
-        const uint32_t nchunks = (s.nc + kScanChunk - 1) / kScanChunk;
-        double rr = 0, rz = 0;
+        const SimDev* sp = w.sims + si;
+        if (sp->solver != 1) continue;
+        const MgLevel L = sp->lev[l + 1];
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t c = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+            if (c >= L.nc) continue;
+            uint16_t info = 0;
+            if (L.type[c] == FLUID) {
+                const int i = int(c % uint32_t(L.nx)), j = int((c / uint32_t(L.nx)) % uint32_t(L.ny));
+                const int kk = int(c / (uint32_t(L.nx) * uint32_t(L.ny)));
+                const int q3[6][3] = {{i - 1, j, kk}, {i + 1, j, kk}, {i, j - 1, kk},
+                                      {i, j + 1, kk}, {i, j, kk - 1}, {i, j, kk + 1}};
+                uint32_t mask = 0, cnt = 0;
 #pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    const int a = q3[q][0], b = q3[q][1], d = q3[q][2];
+                    uint8_t t = SOLID;
+                    if (a >= 0 && b >= 0 && d >= 0 && a < L.nx && b < L.ny && d < L.nz)
+                        t = L.type[uint32_t(a) + uint32_t(L.nx) * (uint32_t(b) + uint32_t(L.ny) * uint32_t(d))];
+                    if (t != SOLID) cnt++;
+                    if (t == FLUID) mask |= 1u << q;
+                }
+                info = uint16_t(mask | (cnt << 8) | 0x8000u);
+            }
+            L.info[c] = info;
+        }
+    }
+}
+
+// ============================================================================ V-cycle
+// One red-black half sweep of A z = r on level l over the cells of one colour.
+// mode 0: z = (r + sum z_n) / cnt; mode 1: the other colour is zero (z = r / cnt);
+// mode 2: as 0 with the coarse correction of level l+1 added to every neighbour on the fly
+// (fused prolongation); mode 3: as 0, then the chunk's partial r.z over all system cells.
+__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode) {
+    __shared__ double sh[8];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev* sp = w.sims + si;
+        if (!active(*sp) || sp->precond != 0) continue;
+        const MgLevel L = sp->lev[l];
+        const int64_t nx = L.nx, nxy = int64_t(L.nx) * L.ny;
+        const uint32_t chunk = item - w.base[si];
+        const MgLevel Cc = (mode == 2) ? sp->lev[l + 1] : L;
         for (int k = 0; k < PER_THREAD; k++) {
             const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc) continue;
-            const uint32_t inf = s.info[c];
+            if (c >= L.nc) continue;
+            const uint32_t inf = L.info[c];
             if (!in_system(inf)) continue;
-            if (zero_x) { s.x64[c] = 0.0; continue; }
-            const float cnt = float((inf >> 8) & 7u);
-            double ax = double(cnt) * s.x64[c];
+            const uint32_t i = c % uint32_t(L.nx), j = (c / uint32_t(L.nx)) % uint32_t(L.ny), kk = c / uint32_t(nxy);
+            if (((i + j + kk) & 1u) != uint32_t(color)) continue;
+            float sum = L.r[c];
+            if (mode != 1) {
 #pragma unroll
-            for (int q = 0; q < 6; q++)
-                if (inf & (1u << q)) ax -= s.x64[int64_t(c) + nbr_off(s, q)];
-            const double rd = -double(rhs_of(s, c)) - ax;
-            const float rf = float(rd);
-            s.r[c] = rf;
-            rr += rd * rd;
-            const float z = rf / cnt;
-            rz += double(rf) * double(z);
-        }
-        block_sum2(rr, rz, sh);
-        if (arrive_last(s, chunk, nchunks, rr, rz, &st->arrive, &last)) {
-            sum_partials(s, nchunks, rr, rz, sh);
-            if (threadIdx.x == 0) {
-                st->arrive = 0;
-                st->restart_now = 0;
-                if (zero_x) {
-                    st->done = 1;
-                    st->status = 3;
-                    st->relres = 0;
-                } else {
-                    const double tol2 = s.rtol * s.rtol * st->bb;
-                    st->relres = sqrt(rr / st->bb);
-                    if (rr <= tol2 || st->iters >= s.max_iter) {
-                        st->done = 1;
-                        st->status = rr <= tol2 ? 0u : 1u;
-                    } else {
-                        st->rz = rz;
-                        st->fresh = 1;
-                        st->since = 0;
+                for (int q = 0; q < 6; q++) {
+                    if (!(inf & (1u << q))) continue;
+                    const int64_t n = int64_t(c) + nbr(q, nx, nxy);
+                    float zn = L.z[n];
+                    if (mode == 2) {
+                        const uint32_t ni = uint32_t(n % nx), nj = uint32_t((n / nx) % L.ny), nk = uint32_t(n / nxy);
+                        const uint32_t P = (ni >> 1) + uint32_t(Cc.nx) * ((nj >> 1) + uint32_t(Cc.ny) * (nk >> 1));
+                        if (in_system(Cc.info[P])) zn += Cc.z[P];
                     }
+                    sum += zn;
                 }
             }
+            L.z[c] = sum / cnt_of(inf);
+        }
+        if (mode == 3) {
+            // r.z over every system cell of the chunk (the other colour was final before this sweep).
+            __syncthreads();
+            DF acc{0.f, 0.f};
+            for (int k = 0; k < PER_THREAD; k++) {
+                const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
+                if (c >= L.nc || !in_system(L.info[c])) continue;
+                acc = df_add(acc, two_prod(L.r[c], L.z[c]));
+            }
+            const double t = block_sum(acc, sh);
+            if (threadIdx.x == 0) sp->partial[chunk] = t;
         }
     }
 }
 
-// -------------------------------------------------------------------------- direction + SpMV
-__device__ __forceinline__ float dir_of(const SimDev& s, const float* __restrict__ pold, int64_t c, uint32_t inf,
-                                        bool fresh, float beta) {
-    const float z = s.r[c] / float((inf >> 8) & 7u);
-    return fresh ? z : z + beta * pold[c];
+// r_{l+1} = 1/2 * sum over the children of their residual r - A z (level l).
+__global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev* sp = w.sims + si;
+        if (!active(*sp) || sp->precond != 0) continue;
+        const MgLevel F = sp->lev[l], Cc = sp->lev[l + 1];
+        const int64_t nx = F.nx, nxy = int64_t(F.nx) * F.ny;
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t P = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+            if (P >= Cc.nc) continue;
+            float sum = 0.0f;
+            if (in_system(Cc.info[P])) {
+                const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
+                const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
+#pragma unroll
+                for (int ch = 0; ch < 8; ch++) {
+                    const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
+                    if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
+                    const int64_t c = int64_t(i) + nx * j + nxy * kk;
+                    const uint32_t inf = F.info[c];
+                    if (!in_system(inf)) continue;
+                    float az = cnt_of(inf) * F.z[c];
+#pragma unroll
+                    for (int q = 0; q < 6; q++)
+                        if (inf & (1u << q)) az -= F.z[c + nbr(q, nx, nxy)];
+                    sum += F.r[c] - az;
+                }
+            }
+            Cc.r[P] = 0.5f * sum;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(THREADS) k_pcg_dir_spmv(Work w) {
-    __shared__ double sh[16];
-    __shared__ bool last;
+// Coarsest level: coarse_iters red-black then black-red iterations from zero, one block per
+// simulation (the level holds at most a few thousand cells).
+__global__ void __launch_bounds__(1024) k_mg_coarse(const SimDev* sims, int n_sims) {
+    for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
+        const SimDev& sr = sims[si];
+        if (sr.solver != 1 || sr.precond != 0 || __ldcg(&sr.pcg->done)) continue;
+        const MgLevel L = sr.lev[sr.nlev - 1];
+        const int64_t nx = L.nx, nxy = int64_t(L.nx) * L.ny;
+        for (uint32_t c = threadIdx.x; c < L.nc; c += blockDim.x) L.z[c] = 0.0f;
+        __syncthreads();
+        const uint32_t iters = sr.coarse_iters;
+        for (uint32_t h = 0; h < 4 * iters; h++) {
+            // colours: (0,1) x iters, then (1,0) x iters
+            const uint32_t color = h < 2 * iters ? (h & 1u) : ((h & 1u) ^ 1u);
+            for (uint32_t c = threadIdx.x; c < L.nc; c += blockDim.x) {
+                const uint32_t inf = L.info[c];
+                if (!in_system(inf)) continue;
+                const uint32_t i = c % uint32_t(L.nx), j = (c / uint32_t(L.nx)) % uint32_t(L.ny), kk = c / uint32_t(nxy);
+                if (((i + j + kk) & 1u) != color) continue;
+                float sum = L.r[c];
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (inf & (1u << q)) sum += L.z[int64_t(c) + nbr(q, nx, nxy)];
+                L.z[c] = sum / cnt_of(inf);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Jacobi preconditioner: z = r / cnt, partial r.z.
+__global__ void __launch_bounds__(THREADS) k_jacobi(Work w) {
+    __shared__ double sh[8];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (s.solver != 1) continue;
-        PcgState* st = s.pcg;
-        if (ld_u32(&st->done)) continue;
+        if (!active(s) || s.precond != 1) continue;
         const uint32_t chunk = item - w.base[si];
-        const uint32_t nchunks = (s.nc + kScanChunk - 1) / kScanChunk;
-        const uint32_t pbuf = ld_u32(&st->pbuf);
-        const float* pold = pbuf ? s.p1 : s.p0;
-        float* pnew = pbuf ? s.p0 : s.p1;
-        const bool fresh = ld_u32(&st->fresh) != 0;
-        const float beta = float(ld_f64(&st->beta));
-        double pap = 0, unused = 0;
-#pragma unroll
+        DF acc{0.f, 0.f};
         for (int k = 0; k < PER_THREAD; k++) {
             const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
             if (c >= s.nc) continue;
             const uint32_t inf = s.info[c];
             if (!in_system(inf)) continue;
-            const float pn = dir_of(s, pold, c, inf, fresh, beta);
-            float ap = float((inf >> 8) & 7u) * pn;
+            const float r = s.r[c];
+            const float z = r / cnt_of(inf);
+            s.z[c] = z;
+            acc = df_add(acc, two_prod(r, z));
+        }
+        const double t = block_sum(acc, sh);
+        if (threadIdx.x == 0) s.partial[chunk] = t;
+    }
+}
+
+// ============================================================================ CG kernels
+// Partial |b|^2.
+__global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) {
+    __shared__ double sh[8];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        if (s.solver != 1) continue;
+        const uint32_t chunk = item - w.base[si];
+        DF acc{0.f, 0.f};
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
+            if (c >= s.nc || !in_system(s.info[c])) continue;
+            const float b = rhs_of(s, c);
+            acc = df_add(acc, two_prod(b, b));
+        }
+        const double t = block_sum(acc, sh);
+        if (threadIdx.x == 0) s.partial[chunk] = t;
+    }
+}
+
+// x64 = hi + lo for simulations about to restart (or x = 0 for a zero right-hand side).
+__global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) {
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        if (!active(s) || !ldu(&s.pcg->restart_now)) continue;
+        const bool zero = ldu(&s.pcg->zero_x) != 0;
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t c = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+            if (c >= s.nc || !in_system(s.info[c])) continue;
+            if (zero) {
+                s.x2[c] = make_float2(0.f, 0.f);
+                s.x64[c] = 0.0;
+            } else {
+                const float2 x = s.x2[c];
+                s.x64[c] = double(x.x) + double(x.y);
+            }
+        }
+    }
+}
+
+// FP64 restart residual r = b - A x and its partial |r|^2.
+__global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) {
+    __shared__ double sh[8];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        if (!active(s) || !ldu(&s.pcg->restart_now) || ldu(&s.pcg->zero_x)) continue;
+        const uint32_t chunk = item - w.base[si];
+        const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
+        double rr = 0;
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
+            if (c >= s.nc) continue;
+            const uint32_t inf = s.info[c];
+            if (!in_system(inf)) continue;
+            double ax = double(cnt_of(inf)) * s.x64[c];
+#pragma unroll
+            for (int q = 0; q < 6; q++)
+                if (inf & (1u << q)) ax -= s.x64[int64_t(c) + nbr(q, nx, nxy)];
+            const double rd = -double(rhs_of(s, c)) - ax;
+            s.r[c] = float(rd);
+            rr += rd * rd;
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) rr += __shfl_down_sync(0xffffffffu, rr, d);
+        if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = rr;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int k2 = 0; k2 < THREADS / 32; k2++) t += sh[k2];
+            s.partial[chunk] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// p' = z + beta p (p' = z after a restart); Ap = A p' (neighbours' p' formed on the fly);
+// partial p'.Ap.
+__global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) {
+    __shared__ double sh[8];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev s = w.sims[si];
+        if (!active(s)) continue;
+        const uint32_t chunk = item - w.base[si];
+        const PcgState* st = s.pcg;
+        const uint32_t pbuf = ldu(&st->pbuf);
+        const float* pold = pbuf ? s.p1 : s.p0;
+        float* pnew = pbuf ? s.p0 : s.p1;
+        const bool fresh = ldu(&st->fresh) != 0;
+        const float beta = float(ldd(&st->beta));
+        const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
+        DF acc{0.f, 0.f};
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
+            if (c >= s.nc) continue;
+            const uint32_t inf = s.info[c];
+            if (!in_system(inf)) continue;
+            const float pn = fresh ? s.z[c] : s.z[c] + beta * pold[c];
+            float ap = cnt_of(inf) * pn;
 #pragma unroll
             for (int q = 0; q < 6; q++) {
                 if (inf & (1u << q)) {
-                    const int64_t nb = int64_t(c) + nbr_off(s, q);
-                    ap -= dir_of(s, pold, nb, s.info[nb], fresh, beta);
+                    const int64_t n = int64_t(c) + nbr(q, nx, nxy);
+                    ap -= fresh ? s.z[n] : s.z[n] + beta * pold[n];
                 }
             }
             pnew[c] = pn;
             s.Ap[c] = ap;
-            pap += double(pn) * double(ap);
+            acc = df_add(acc, two_prod(pn, ap));
         }
-        block_sum2(pap, unused, sh);
-        if (arrive_last(s, chunk, nchunks, pap, 0.0, &st->arrive, &last)) {
-            sum_partials(s, nchunks, pap, unused, sh);
-            if (threadIdx.x == 0) {
-                st->arrive = 0;
-                st->pbuf ^= 1u;   // p' is now the current direction
-                st->pAp = pap;
-                if (!(pap > 0.0)) {
-                    st->done = 1;
-                    st->status = 2;
-                } else {
-                    st->alpha = st->rz / pap;
-                }
-            }
-        }
+        const double t = block_sum(acc, sh);
+        if (threadIdx.x == 0) s.partial[chunk] = t;
     }
 }
 
-// -------------------------------------------------------------------------- update
+// x += alpha p (double-float), r -= alpha Ap (FP32), partial |r|^2.
 __global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) {
-    __shared__ double sh[16];
-    __shared__ bool last;
+    __shared__ double sh[8];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (s.solver != 1) continue;
-        PcgState* st = s.pcg;
-        if (ld_u32(&st->done)) continue;
+        if (!active(s)) continue;
         const uint32_t chunk = item - w.base[si];
-        const uint32_t nchunks = (s.nc + kScanChunk - 1) / kScanChunk;
-        const uint32_t pbuf = ld_u32(&st->pbuf);
-        const float* p = pbuf ? s.p1 : s.p0;
-        const double alpha = ld_f64(&st->alpha);
-        const float af = float(alpha);
-        double rr = 0, rzn = 0;
-#pragma unroll
+        const PcgState* st = s.pcg;
+        const float* p = ldu(&st->pbuf) ? s.p1 : s.p0;
+        const float ah = ldf(&st->alpha_hi), al = ldf(&st->alpha_lo);
+        const float af = float(ldd(&st->alpha));
+        DF acc{0.f, 0.f};
         for (int k = 0; k < PER_THREAD; k++) {
             const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc) continue;
-            const uint32_t inf = s.info[c];
-            if (!in_system(inf)) continue;
+            if (c >= s.nc || !in_system(s.info[c])) continue;
             const float pc = p[c];
-            s.x64[c] += alpha * double(pc);
+            DF d = two_prod(ah, pc);
+            d.lo += al * pc;
+            const float2 x = s.x2[c];
+            const DF xn = df_add(DF{x.x, x.y}, d);
+            s.x2[c] = make_float2(xn.hi, xn.lo);
             const float rn = s.r[c] - af * s.Ap[c];
             s.r[c] = rn;
-            const float z = rn / float((inf >> 8) & 7u);
-            rr += double(rn) * double(rn);
-            rzn += double(rn) * double(z);
+            acc = df_add(acc, two_prod(rn, rn));
         }
-        block_sum2(rr, rzn, sh);
-        if (arrive_last(s, chunk, nchunks, rr, rzn, &st->arrive, &last)) {
-            sum_partials(s, nchunks, rr, rzn, sh);
-            if (threadIdx.x == 0) {
-                st->arrive = 0;
-                st->iters += 1;
-                st->since += 1;
-                st->rr = rr;
-                st->rzn = rzn;
-                const double tol2 = s.rtol * s.rtol * st->bb;
-                if (rr <= tol2 || st->since >= s.restart || st->iters >= s.max_iter) {
-                    st->restart_now = 1;
-                } else {
-                    st->beta = rzn / st->rz;
-                    st->rz = rzn;
-                    st->fresh = 0;
-                }
-            }
-        }
+        const double t = block_sum(acc, sh);
+        if (threadIdx.x == 0) s.partial[chunk] = t;
     }
 }
 
-// -------------------------------------------------------------------------- finish / condition
+// FP32 pressure copy and the FP64 solution at the end of the solve.
 __global__ void __launch_bounds__(THREADS) k_pcg_finish(Work w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
-#pragma unroll
         for (int k = 0; k < PER_THREAD; k++) {
             const uint32_t c = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
-            if (c < s.nc) s.pressure[c] = float(s.x64[c]);
+            if (c >= s.nc) continue;
+            double x = 0.0;
+            if (in_system(s.info[c])) {
+                const float2 v = s.x2[c];
+                x = double(v.x) + double(v.y);
+            }
+            s.x64[c] = x;
+            s.pressure[c] = float(x);
+        }
+    }
+}
+
+// ============================================================================ control kernels
+// One block per simulation; each sums the partials of the step before it and advances the state.
+// phase 0: after |b|^2   1: after the restart residual   2: after r.z   3: after p.Ap   4: after |r|^2
+__global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_sims, int phase) {
+    __shared__ double sh[8];
+    for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
+        const SimDev& s = sims[si];
+        if (s.solver != 1) continue;
+        PcgState* st = s.pcg;
+        if (phase != 0 && __ldcg(&st->done)) continue;
+        if (phase == 1 && !__ldcg(&st->restart_now)) continue;
+        const bool zero = phase == 1 && __ldcg(&st->zero_x);
+        const double a = zero ? 0.0 : sum_partials(s, sh);
+        if (threadIdx.x == 0) switch (phase) {
+            case 0:
+                st->bb = a;
+                st->iters = 0;
+                st->since = 0;
+                st->done = 0;
+                st->fresh = 1;
+                st->status = 0;
+                st->relres = 0;
+                st->beta = 0;
+                st->restart_now = 1;
+                st->zero_x = a == 0.0 ? 1u : 0u;
+                break;
+            case 1:
+                if (zero) {
+                    st->done = 1;
+                    st->status = 3;
+                    st->relres = 0;
+                } else {
+                    const double tol2 = s.rtol * s.rtol * st->bb;
+                    st->relres = sqrt(a / st->bb);
+                    if (a <= tol2 || st->iters >= s.max_iter) {
+                        st->done = 1;
+                        st->status = a <= tol2 ? 0u : 1u;
+                    }
+                }
+                break;
+            case 2:
+                if (st->restart_now) {
+                    st->rz = a;
+                    st->fresh = 1;
+                    st->since = 0;
+                    st->restart_now = 0;
+                } else {
+                    st->beta = a / st->rz;
+                    st->rz = a;
+                    st->fresh = 0;
+                }
+                break;
+            case 3:
+                st->pAp = a;
+                st->pbuf ^= 1u;   // p' is now the current direction
+                if (!(a > 0.0)) {
+                    st->done = 1;
+                    st->status = 2;
+                } else {
+                    const double alpha = st->rz / a;
+                    st->alpha = alpha;
+                    st->alpha_hi = float(alpha);
+                    st->alpha_lo = float(alpha - double(float(alpha)));
+                }
+                break;
+            default: {
+                const double tol2 = s.rtol * s.rtol * st->bb;
+                st->rr = a;
+                st->iters += 1;
+                st->since += 1;
+                if (a <= tol2 || st->since >= s.restart || st->iters >= s.max_iter) st->restart_now = 1;
+                break;
+            }
         }
     }
 }
@@ -340,7 +586,7 @@ __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
     *flag = any;
 }
 
-// -------------------------------------------------------------------------- launchers
+// ============================================================================ launchers
 static unsigned grid_of(uint32_t total) {
     const uint32_t cap = uint32_t(sm_count() * 8);
     return total < cap ? (total ? total : 1u) : cap;
@@ -355,32 +601,68 @@ static inline Work mkw(const StageWork& sw) {
     return w;
 }
 
-cudaError_t launch_pcg_init(const StageWork& chunks, cudaStream_t st) {
-    k_pcg_init<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
-    k_pcg_restart<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
+static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st) {
+    k_pcg_ctl<<<pw.n_sims, THREADS, 0, st>>>(pw.sims, pw.n_sims, phase);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pcg_body(const StageWork& chunks, cudaStream_t st) {
-    k_pcg_dir_spmv<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
-    k_pcg_update<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
-    k_pcg_restart<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
+cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
+    for (int l = 0; l + 1 < pw.max_levels; l++) {
+        if (!pw.coarse[l].total) continue;
+        k_mg_coarsen<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
+        k_mg_info<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_pcg_dir_spmv(const StageWork& chunks, cudaStream_t st) {
-    k_pcg_dir_spmv<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
-    return cudaGetLastError();
+cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
+    if (pw.any_jacobi) k_jacobi<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    if (pw.any_mg) {
+        for (int l = 0; l + 1 < pw.max_levels; l++) {
+            if (!pw.level[l].total) continue;
+            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 0, 1);
+            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 1, 0);
+            k_mg_restrict<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
+        }
+        k_mg_coarse<<<pw.n_sims, 1024, 0, st>>>(pw.sims, pw.n_sims);
+        for (int l = pw.max_levels - 2; l >= 0; l--) {
+            if (!pw.level[l].total) continue;
+            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 1, 2);
+            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 0, l == 0 ? 3 : 0);
+        }
+    }
+    return ctl(pw, 2, st);
 }
 
-cudaError_t launch_pcg_update(const StageWork& chunks, cudaStream_t st) {
-    k_pcg_update<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
-    return cudaGetLastError();
+cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st) {
+    k_pcg_widen<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    k_pcg_resid<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    return ctl(pw, 1, st);
 }
 
-cudaError_t launch_pcg_restart(const StageWork& chunks, cudaStream_t st) {
-    k_pcg_restart<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
-    return cudaGetLastError();
+cudaError_t launch_pcg_init(const PcgWork& pw, cudaStream_t st) {
+    launch_mg_setup(pw, st);
+    k_pcg_init<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    ctl(pw, 0, st);
+    launch_pcg_restart(pw, st);
+    return launch_precond(pw, st);
+}
+
+cudaError_t launch_pcg_dir(const PcgWork& pw, cudaStream_t st) {
+    k_pcg_dir<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    return ctl(pw, 3, st);
+}
+
+cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st) {
+    k_pcg_update<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    return ctl(pw, 4, st);
+}
+
+cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st) {
+    launch_pcg_dir(pw, st);
+    launch_pcg_update(pw, st);
+    launch_pcg_restart(pw, st);
+    return launch_precond(pw, st);
 }
 
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {
@@ -393,8 +675,8 @@ cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaS
     return cudaGetLastError();
 }
 
-cudaError_t launch_pcg_finish(const StageWork& chunks, cudaStream_t st) {
-    k_pcg_finish<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks));
+cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st) {
+    k_pcg_finish<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
     return cudaGetLastError();
 }
 

@@ -10,7 +10,8 @@
 //   cells      type u8, start u32 (C + 1, exclusive scan of per-cell counts), count u32,
 //              pressure f32, div f32, info u16 (fluid-neighbour mask | non-solid count << 8 |
 //              fluid << 15)
-//   precision  x64 f64, r f32, p (two f32 buffers), Ap f32
+//   precision  x2 double-float pair, x64 f64, r z p0 p1 Ap f32, per-chunk partials, and the
+//              multigrid levels (type u8, info u16, r z f32 per coarse cell)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -19,26 +20,35 @@ namespace pxf {
 
 enum : uint8_t { AIR = 0, FLUID = 1, SOLID = 2 };   // fluid.slang:40
 
-// Per-simulation scalars of the precision (PCG) solver.
+// Per-simulation scalars of the precision (PCG) solver, written by one-block control kernels.
 struct PcgState {
     double bb;        // |b|^2
     double rz;        // r.z of the current direction
     double pAp;
     double rr;        // recurrence |r|^2
-    double rzn;       // r.z after the update
     double alpha, beta;
     double relres;    // last FP64 restart residual / |b|
-    uint32_t iters;   // total PCG steps this solve
+    uint32_t iters;   // PCG steps this solve
     uint32_t since;   // steps since the last restart
-    uint32_t done;    // 1 when converged, capped or broken down
-    uint32_t fresh;   // 1 right after a restart: next direction p = z
+    uint32_t done;    // converged, capped, broken down or zero rhs
+    uint32_t fresh;   // the next direction is p = z
     uint32_t restart_now;
     uint32_t status;  // 0 converged, 1 iteration cap, 2 breakdown, 3 zero rhs
-    uint32_t arrive;  // chunks of the current launch that have finished (last-block reduction)
     uint32_t pbuf;    // which of p0 / p1 holds the current direction
     uint32_t zero_x;  // zero right-hand side: the solution is x = 0
-    uint32_t pad;
+    float alpha_hi, alpha_lo;   // alpha as a double-float pair
 };
+
+// One level of the multigrid hierarchy (level 0 aliases the simulation's own arrays).
+struct MgLevel {
+    int nx, ny, nz;
+    uint32_t nc;
+    uint8_t* type;
+    uint16_t* info;
+    float* r;
+    float* z;
+};
+constexpr int kMaxLevels = 12;
 
 struct SimDev {
     int nx, ny, nz;
@@ -49,6 +59,8 @@ struct SimDev {
     uint32_t nu, nv, nw, nf, nc;
     uint32_t iterations;     // red-black GS iterations
     uint32_t solver;         // 0 red-black GS, 1 precision PCG
+    uint32_t precond;        // precision PCG preconditioner: 0 multigrid V-cycle, 1 Jacobi
+    uint32_t coarse_iters;   // symmetric red-black iterations on the coarsest level
     double rtol;
     uint32_t max_iter, restart;
     float4 *posA, *velA, *posB, *velB;
@@ -57,10 +69,14 @@ struct SimDev {
     uint32_t *count, *start, *chunk;
     uint16_t* info;
     int32_t *acc, *wacc;     // optional copies of the P2G fixed-point sums
-    double* x64;
-    float *r, *p0, *p1, *Ap;
-    double* partial;         // per-block partial sums of the precision solver
+    // precision solver
+    float2* x2;              // solution as a double-float pair (hi, lo)
+    double* x64;             // FP64 solution, written at restarts and at the end of the solve
+    float *r, *z, *p0, *p1, *Ap;
+    double* partial;         // two partial sums per 2048-cell chunk of level 0
     PcgState* pcg;
+    int nlev;
+    MgLevel lev[kMaxLevels];
 };
 
 // Work index of one stage over a batch: item i of the stage belongs to simulation s where

@@ -17,6 +17,7 @@ struct StageWork {
 
 constexpr uint32_t kScanChunk = 2048;     // cells per scan / precision-solver work item
 constexpr uint32_t kElemItem = 256;       // elements per item of the per-element kernels
+constexpr int kMaxLevelsK = 12;           // multigrid levels (kMaxLevels in pxf_device.cuh)
 
 int sm_count();
 void p2g_shape(int shape, int out[3]);
@@ -35,18 +36,29 @@ cudaError_t launch_gather_aos(const SimDev& s, float4* out, cudaStream_t st);
 cudaError_t launch_scatter_aos(const SimDev& s, const float4* in, cudaStream_t st);
 cudaError_t launch_counts_from_start(const SimDev& s, uint32_t* out, cudaStream_t st);
 
-// Precision solver: init (|b|^2, state reset) and one restart, then the loop body
-// (direction + SpMV, update, conditional restart) repeated while any simulation runs; finish
-// writes the FP32 pressure copy.
-cudaError_t launch_pcg_init(const StageWork& chunks, cudaStream_t st);
-cudaError_t launch_pcg_body(const StageWork& chunks, cudaStream_t st);
+// Work indexes of the precision solver for one batch.
+struct PcgWork {
+    const SimDev* sims = nullptr;
+    int n_sims = 0;
+    StageWork chunks;                 // level-0 chunks of kScanChunk cells (precision simulations)
+    StageWork level[kMaxLevelsK];     // level-l chunks of multigrid simulations with a level below l
+    StageWork coarse[kMaxLevelsK];    // level-(l+1) chunks of those simulations
+    int max_levels = 0;
+    bool any_mg = false, any_jacobi = false;
+};
+
+// Precision solver: multigrid setup + |b|^2 + state reset + first restart + first z = M^-1 r;
+// then the loop body (direction + SpMV, update, conditional FP64 restart, preconditioner) while
+// any simulation runs; finish writes the FP64 solution and the FP32 pressure copy.
+cudaError_t launch_pcg_init(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_pcg_dir(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
-cudaError_t launch_pcg_finish(const StageWork& chunks, cudaStream_t st);
-// The loop body's three kernels, launched one by one (stage profiling).
-cudaError_t launch_pcg_dir_spmv(const StageWork& chunks, cudaStream_t st);
-cudaError_t launch_pcg_update(const StageWork& chunks, cudaStream_t st);
-cudaError_t launch_pcg_restart(const StageWork& chunks, cudaStream_t st);
-// Host-driven fallback: one loop body + a flag telling whether any simulation still runs.
+// Host-driven fallback: a flag telling whether any simulation still runs.
 cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaStream_t st);
 
 }  // namespace pxf

@@ -133,7 +133,10 @@ __global__ void __launch_bounds__(256) k_scan_apply(Work w) {
                 s.type[c] = t;
                 if (t != FLUID) {
                     s.pressure[c] = 0.0f;
-                    if (s.x64) s.x64[c] = 0.0;
+                    if (s.x2) {
+                        s.x2[c] = make_float2(0.0f, 0.0f);
+                        s.x64[c] = 0.0;
+                    }
                 }
             }
         }
