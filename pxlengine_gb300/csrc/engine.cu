@@ -226,7 +226,7 @@ static inline uint32_t cdiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1
 
 // Work-index stages: particles, P2G tiles, cells, half cells, faces, 2048-cell chunks, then the
 // multigrid smoothing chunks of each level and the restriction chunks of each level.
-constexpr int kStages = 6 + 2 * kMaxLevels;
+constexpr int kStages = 6 + 3 * kMaxLevels;
 
 int BatchImpl::rebuild() {
     cudaError_t e;
@@ -270,10 +270,11 @@ int BatchImpl::rebuild() {
             cdiv(d.nc, kScanChunk)};
         const bool mg = d.solver == 1 && d.precond == 0;
         for (int l = 0; l < kMaxLevels; l++) {
-            // level l smoothing and restriction to l + 1 exist when level l is not the coarsest
-            const bool has = mg && l + 1 < d.nlev;
+            // global-memory smoothing of level l and restriction to l + 1 exist below the tail
+            const bool has = mg && l < d.tail;
             items[6 + l] = has ? cdiv(d.lev[l].nc, kScanChunk) : 0;
             items[6 + kMaxLevels + l] = has ? cdiv(d.lev[l + 1].nc, kScanChunk) : 0;
+            items[6 + 2 * kMaxLevels + l] = (mg && l + 1 < d.nlev) ? cdiv(d.lev[l + 1].nc, kScanChunk) : 0;
         }
         for (int k = 0; k < kStages; k++) base[k * (n + 1) + i + 1] = base[k * (n + 1) + i] + items[k];
         if (d.solver == 0) {
@@ -281,7 +282,14 @@ int BatchImpl::rebuild() {
             max_gs_iters = std::max(max_gs_iters, d.iterations);
         } else {
             any_pcg = true;
-            if (mg) { pw.any_mg = true; pw.max_levels = std::max(pw.max_levels, d.nlev); }
+            if (mg) {
+                pw.any_mg = true;
+                pw.max_levels = std::max(pw.max_levels, d.tail + 1);
+                pw.setup_levels = std::max(pw.setup_levels, d.nlev);
+                size_t bytes = 0;
+                for (int l = d.tail; l < d.nlev; l++) bytes += 4 * (2 * size_t(d.lev[l].nc) + (d.lev[l].nc + 1) / 2);
+                pw.tail_smem = std::max(pw.tail_smem, bytes);
+            }
             else pw.any_jacobi = true;
         }
         timeout_s = std::max(timeout_s, s->opts.wait_timeout_s);
@@ -297,6 +305,7 @@ int BatchImpl::rebuild() {
     for (int l = 0; l < kMaxLevels; l++) {
         ws[6 + l] = &pw.level[l];
         ws[6 + kMaxLevels + l] = &pw.coarse[l];
+        ws[6 + 2 * kMaxLevels + l] = &pw.setup[l];
     }
     for (int k = 0; k < kStages; k++) {
         ws[k]->sims = d_sims;
@@ -307,6 +316,7 @@ int BatchImpl::rebuild() {
     pw.sims = d_sims;
     pw.n_sims = n;
     pw.chunks = w_chunks;
+    if (pw.any_mg && (e = mg_tail_attr(pw.tail_smem)) != cudaSuccess) return cuda_fail(e, "tail kernel attribute");
     int rc = capture();
     if (rc) return rc;
     dirty = false;
@@ -719,6 +729,8 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
         d.partial = reinterpret_cast<double*>(m + L.partial);
         d.pcg = reinterpret_cast<PcgState*>(m + L.pcg);
         d.nlev = L.nlev > 0 ? L.nlev : 1;
+        d.tail = 0;
+        while (d.tail + 1 < d.nlev && uint64_t(L.dims[d.tail][0]) * L.dims[d.tail][1] * L.dims[d.tail][2] > kTailCells) d.tail++;
         d.lev[0].nx = d.nx; d.lev[0].ny = d.ny; d.lev[0].nz = d.nz;
         d.lev[0].nc = d.nc;
         d.lev[0].type = d.type;

@@ -190,26 +190,30 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
         const SimDev* sp = w.sims + si;
         if (!active(*sp) || sp->precond != 0) continue;
         const MgLevel L = sp->lev[l];
-        const int64_t nx = L.nx, nxy = int64_t(L.nx) * L.ny;
+        const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
         const uint32_t chunk = item - w.base[si];
         const MgLevel Cc = (mode == 2) ? sp->lev[l + 1] : L;
+        const uint32_t cnx = uint32_t(Cc.nx), cnxy = uint32_t(Cc.nx) * uint32_t(Cc.ny);
         for (int k = 0; k < PER_THREAD; k++) {
             const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
             if (c >= L.nc) continue;
             const uint32_t inf = L.info[c];
             if (!in_system(inf)) continue;
-            const uint32_t i = c % uint32_t(L.nx), j = (c / uint32_t(L.nx)) % uint32_t(L.ny), kk = c / uint32_t(nxy);
+            const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
             if (((i + j + kk) & 1u) != uint32_t(color)) continue;
             float sum = L.r[c];
             if (mode != 1) {
 #pragma unroll
                 for (int q = 0; q < 6; q++) {
                     if (!(inf & (1u << q))) continue;
-                    const int64_t n = int64_t(c) + nbr(q, nx, nxy);
+                    const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                    const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                    const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                    const uint32_t n = uint32_t(int64_t(c) + dx + int64_t(dy) * nx + int64_t(dz) * nxy);
                     float zn = L.z[n];
                     if (mode == 2) {
-                        const uint32_t ni = uint32_t(n % nx), nj = uint32_t((n / nx) % L.ny), nk = uint32_t(n / nxy);
-                        const uint32_t P = (ni >> 1) + uint32_t(Cc.nx) * ((nj >> 1) + uint32_t(Cc.ny) * (nk >> 1));
+                        const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
+                                           cnxy * (uint32_t(int(kk) + dz) >> 1);
                         if (in_system(Cc.info[P])) zn += Cc.z[P];
                     }
                     sum += zn;
@@ -266,33 +270,143 @@ __global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
     }
 }
 
-// Coarsest level: coarse_iters red-black then black-red iterations from zero, one block per
-// simulation (the level holds at most a few thousand cells).
-__global__ void __launch_bounds__(1024) k_mg_coarse(const SimDev* sims, int n_sims) {
-    for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
-        const SimDev& sr = sims[si];
-        if (sr.solver != 1 || sr.precond != 0 || __ldcg(&sr.pcg->done)) continue;
-        const MgLevel L = sr.lev[sr.nlev - 1];
-        const int64_t nx = L.nx, nxy = int64_t(L.nx) * L.ny;
-        for (uint32_t c = threadIdx.x; c < L.nc; c += blockDim.x) L.z[c] = 0.0f;
-        __syncthreads();
-        const uint32_t iters = sr.coarse_iters;
-        for (uint32_t h = 0; h < 4 * iters; h++) {
-            // colours: (0,1) x iters, then (1,0) x iters
-            const uint32_t color = h < 2 * iters ? (h & 1u) : ((h & 1u) ^ 1u);
-            for (uint32_t c = threadIdx.x; c < L.nc; c += blockDim.x) {
-                const uint32_t inf = L.info[c];
+// ------------------------------------------------------------------ shared-memory tail
+// Levels tail..nlev-1 (the tail level holds at most kTailCells cells) run as one V-cycle inside
+// one block, in shared memory: same sweeps, restriction, fused prolongation and coarsest solve as
+// the global-memory path. Input r of the tail level, output z of the tail level; when the tail is
+// level 0 the block also writes the level-0 chunk partials of r.z.
+struct TailLevel {
+    int nx, ny, nz;
+    uint32_t nc;
+    float* r;
+    float* z;
+    uint16_t* info;
+};
+
+__device__ void tail_smooth(const TailLevel& L, uint32_t color, int mode, const TailLevel* C) {
+    const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
+    for (uint32_t c = threadIdx.x; c < L.nc; c += blockDim.x) {
+        const uint32_t inf = L.info[c];
+        if (!in_system(inf)) continue;
+        const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
+        if (((i + j + kk) & 1u) != color) continue;
+        float sum = L.r[c];
+        if (mode != 1) {
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                if (!(inf & (1u << q))) continue;
+                const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                const uint32_t n = uint32_t(int(c) + dx + dy * int(nx) + dz * int(nxy));
+                float zn = L.z[n];
+                if (mode == 2) {
+                    const uint32_t P = (uint32_t(int(i) + dx) >> 1) + uint32_t(C->nx) * ((uint32_t(int(j) + dy) >> 1) +
+                                       uint32_t(C->ny) * (uint32_t(int(kk) + dz) >> 1));
+                    if (in_system(C->info[P])) zn += C->z[P];
+                }
+                sum += zn;
+            }
+        }
+        L.z[c] = sum / cnt_of(inf);
+    }
+    __syncthreads();
+}
+
+__device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc) {
+    const uint32_t nx = uint32_t(F.nx), nxy = uint32_t(F.nx) * uint32_t(F.ny);
+    for (uint32_t P = threadIdx.x; P < Cc.nc; P += blockDim.x) {
+        float sum = 0.0f;
+        if (in_system(Cc.info[P])) {
+            const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
+            const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
+#pragma unroll
+            for (int ch = 0; ch < 8; ch++) {
+                const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
+                if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
+                const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
+                const uint32_t inf = F.info[c];
                 if (!in_system(inf)) continue;
-                const uint32_t i = c % uint32_t(L.nx), j = (c / uint32_t(L.nx)) % uint32_t(L.ny), kk = c / uint32_t(nxy);
-                if (((i + j + kk) & 1u) != color) continue;
-                float sum = L.r[c];
+                float az = cnt_of(inf) * F.z[c];
 #pragma unroll
                 for (int q = 0; q < 6; q++)
-                    if (inf & (1u << q)) sum += L.z[int64_t(c) + nbr(q, nx, nxy)];
-                L.z[c] = sum / cnt_of(inf);
+                    if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+                sum += F.r[c] - az;
             }
-            __syncthreads();
         }
+        Cc.r[P] = 0.5f * sum;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims) {
+    extern __shared__ float tsm[];
+    __shared__ double sh[32];
+    for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
+        const SimDev* sp = sims + si;
+        if (sp->solver != 1 || sp->precond != 0 || __ldcg(&sp->pcg->done)) continue;
+        const int T = sp->tail, NL = sp->nlev;
+        TailLevel lv[kMaxLevels];
+        // shared layout per level: r, z (float), info (u16, padded to floats)
+        float* base = tsm;
+        for (int l = T; l < NL; l++) {
+            const MgLevel g = sp->lev[l];
+            lv[l].nx = g.nx; lv[l].ny = g.ny; lv[l].nz = g.nz; lv[l].nc = g.nc;
+            lv[l].r = base;
+            lv[l].z = base + g.nc;
+            lv[l].info = reinterpret_cast<uint16_t*>(base + 2 * g.nc);
+            base += 2 * g.nc + (g.nc + 1) / 2;
+            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[l].info[c] = g.info[c];
+        }
+        {
+            const MgLevel g = sp->lev[T];
+            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[T].r[c] = g.r[c];
+        }
+        __syncthreads();
+        for (int l = T; l + 1 < NL; l++) {
+            tail_smooth(lv[l], 0, 1, nullptr);
+            tail_smooth(lv[l], 1, 0, nullptr);
+            tail_restrict(lv[l], lv[l + 1]);
+        }
+        {
+            const TailLevel& Lc = lv[NL - 1];
+            for (uint32_t c = threadIdx.x; c < Lc.nc; c += blockDim.x) Lc.z[c] = 0.0f;
+            __syncthreads();
+            const uint32_t it = sp->coarse_iters;
+            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, 0, 0, nullptr); tail_smooth(Lc, 1, 0, nullptr); }
+            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, 1, 0, nullptr); tail_smooth(Lc, 0, 0, nullptr); }
+        }
+        for (int l = NL - 2; l >= T; l--) {
+            tail_smooth(lv[l], 1, 2, &lv[l + 1]);
+            tail_smooth(lv[l], 0, 0, nullptr);
+        }
+        {
+            const MgLevel g = sp->lev[T];
+            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) g.z[c] = lv[T].z[c];
+        }
+        if (T == 0) {
+            // level-0 chunk partials of r.z (the tail holds the whole level)
+            const uint32_t nch = (sp->nc + kScanChunk - 1) / kScanChunk;
+            for (uint32_t ch = 0; ch < nch; ch++) {
+                DF acc{0.f, 0.f};
+                for (uint32_t c = ch * kScanChunk + threadIdx.x; c < min((ch + 1) * kScanChunk, sp->nc); c += blockDim.x)
+                    if (in_system(lv[0].info[c])) acc = df_add(acc, two_prod(lv[0].r[c], lv[0].z[c]));
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) {
+                    const DF t{__shfl_down_sync(0xffffffffu, acc.hi, d), __shfl_down_sync(0xffffffffu, acc.lo, d)};
+                    acc = df_add(acc, t);
+                }
+                if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = double(acc.hi) + double(acc.lo);
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    double t = 0;
+                    for (int k = 0; k < int(blockDim.x >> 5); k++) t += sh[k];
+                    sp->partial[ch] = t;
+                }
+                __syncthreads();
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -606,11 +720,15 @@ static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+cudaError_t mg_tail_attr(size_t smem) {
+    return cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+}
+
 cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
-    for (int l = 0; l + 1 < pw.max_levels; l++) {
-        if (!pw.coarse[l].total) continue;
-        k_mg_coarsen<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
-        k_mg_info<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
+    for (int l = 0; l + 1 < pw.setup_levels; l++) {
+        if (!pw.setup[l].total) continue;
+        k_mg_coarsen<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l);
+        k_mg_info<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l);
     }
     return cudaGetLastError();
 }
@@ -624,7 +742,7 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
             k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 1, 0);
             k_mg_restrict<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
         }
-        k_mg_coarse<<<pw.n_sims, 1024, 0, st>>>(pw.sims, pw.n_sims);
+        k_mg_tail<<<pw.n_sims, 1024, pw.tail_smem, st>>>(pw.sims, pw.n_sims);
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
             k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 1, 2);

@@ -76,6 +76,7 @@ struct SimDev {
     double* partial;         // two partial sums per 2048-cell chunk of level 0
     PcgState* pcg;
     int nlev;
+    int tail;                // first level handled by the shared-memory tail kernel
     MgLevel lev[kMaxLevels];
 };
 

@@ -43,9 +43,15 @@ struct PcgWork {
     StageWork chunks;                 // level-0 chunks of kScanChunk cells (precision simulations)
     StageWork level[kMaxLevelsK];     // level-l chunks of multigrid simulations with a level below l
     StageWork coarse[kMaxLevelsK];    // level-(l+1) chunks of those simulations
-    int max_levels = 0;
+    StageWork setup[kMaxLevelsK];     // level-(l+1) chunks of every multigrid simulation with level l+1
+    int setup_levels = 0;
+    int max_levels = 0;                 // global-memory levels (below the shared-memory tail)
     bool any_mg = false, any_jacobi = false;
+    size_t tail_smem = 0;               // dynamic shared memory of the tail kernel
 };
+
+constexpr uint32_t kTailCells = 8192;   // the shared-memory tail starts at the first level this small
+cudaError_t mg_tail_attr(size_t smem);
 
 // Precision solver: multigrid setup + |b|^2 + state reset + first restart + first z = M^-1 r;
 // then the loop body (direction + SpMV, update, conditional FP64 restart, preconditioner) while

@@ -255,28 +255,38 @@ __global__ void __launch_bounds__(256) k_p2g(Work w) {
                 const float vv[3] = {V.x, V.y, V.z};
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    float gq[3];
-                    int b[3];
+                    // Box of this component's owned faces: SDX x SDY x (TZ + (c == 2)) in shared memory.
+                    const int SDX = c == 0 ? TX + 1 : TX;
+                    const int SDY = c == 1 ? TY + 1 : TY;
+                    int lb[3];
                     float wt[3][2];
+                    bool ok[3][2];
 #pragma unroll
                     for (int a = 0; a < 3; a++) {
-                        gq[a] = (x[a] - s.o[a]) * s.inv_h - 0.5f;
-                        if (a == c) gq[a] += 0.5f;
-                        b[a] = f2i(floorf(gq[a]));
-                        const float f = gq[a] - float(b[a]);
+                        float gq = (x[a] - s.o[a]) * s.inv_h - 0.5f;
+                        if (a == c) gq += 0.5f;
+                        const int b = f2i(floorf(gq));
+                        const float f = gq - float(b);
                         wt[a][0] = fmix(1.0f - f, f, 0.0f);
                         wt[a][1] = fmix(1.0f - f, f, 1.0f);
-                        b[a] -= org[a];
+                        lb[a] = b - org[a];
+                        ok[a][0] = unsigned(lb[a]) < unsigned(E[c][a]);
+                        ok[a][1] = unsigned(lb[a] + 1) < unsigned(E[c][a]);
                     }
+                    if (!((ok[0][0] | ok[0][1]) & (ok[1][0] | ok[1][1]) & (ok[2][0] | ok[2][1]))) continue;
+                    // w = (wx * wy) * wz, the reference's product order
+                    const float wxy[2][2] = {{wt[0][0] * wt[1][0], wt[0][0] * wt[1][1]},
+                                             {wt[0][1] * wt[1][0], wt[0][1] * wt[1][1]}};
+                    const int base = sbase[c] + lb[0] + SDX * (lb[1] + SDY * lb[2]);
+                    const float v = vv[c];
 #pragma unroll
                     for (int k = 0; k < 8; k++) {
                         const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
-                        const int lx = b[0] + ox, ly = b[1] + oy, lz = b[2] + oz;
-                        if (lx < 0 || ly < 0 || lz < 0 || lx >= E[c][0] || ly >= E[c][1] || lz >= E[c][2]) continue;
-                        const float wgt = wt[0][ox] * wt[1][oy] * wt[2][oz];
-                        const int si2 = sbase[c] + lx + sdx[c] * (ly + sdy[c] * lz);
-                        atomicAdd(&sacc[si2], f2i(wgt * vv[c] * SW));
-                        atomicAdd(&swac[si2], f2i(wgt * SW));
+                        if (!(ok[0][ox] & ok[1][oy] & ok[2][oz])) continue;
+                        const float wgt = wxy[ox][oy] * wt[2][oz];
+                        const int idx = base + ox + SDX * oy + SDX * SDY * oz;
+                        atomicAdd(&sacc[idx], f2i(wgt * v * SW));
+                        atomicAdd(&swac[idx], f2i(wgt * SW));
                     }
                 }
             }
@@ -421,35 +431,57 @@ __global__ void __launch_bounds__(256) k_project(Work w) {
 }
 
 // ------------------------------------------------------------------ G2P + advection + binning
-// fluid.slang:67-84 (trilinear sampling with clamped indices) and 199-220.
-__device__ __forceinline__ float sample_face(const SimDev& s, const float* __restrict__ buf, int c, float x,
-                                             float y, float z) {
+// fluid.slang:67-84 (trilinear sampling with clamped indices) and 199-220. Both buffers are
+// sampled with one index/weight computation; when every tap lies inside the face grid the clamp
+// is the identity and the taps use constant offsets (same values, same summation order).
+struct Taps {
+    float w[8];
+    uint32_t idx[8];
+};
+
+__device__ __forceinline__ void face_taps(const SimDev& s, int c, float x, float y, float z, Taps& t) {
     const float xs[3] = {x, y, z};
     const int n[3] = {s.nx, s.ny, s.nz};
-    float g[3];
     int b[3], d[3];
     float wt[3][2];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        g[a] = (xs[a] - s.o[a]) * s.inv_h - 0.5f;
-        if (a == c) g[a] += 0.5f;
-        b[a] = f2i(floorf(g[a]));
-        const float f = g[a] - float(b[a]);
+        float g = (xs[a] - s.o[a]) * s.inv_h - 0.5f;
+        if (a == c) g += 0.5f;
+        b[a] = f2i(floorf(g));
+        const float f = g - float(b[a]);
         wt[a][0] = fmix(1.0f - f, f, 0.0f);
         wt[a][1] = fmix(1.0f - f, f, 1.0f);
         d[a] = n[a] + (a == c) - 1;
     }
     const uint32_t fdx = uint32_t(d[0] + 1), fdy = uint32_t(d[1] + 1);
+    const bool inside = b[0] >= 0 && b[1] >= 0 && b[2] >= 0 && b[0] < d[0] && b[1] < d[1] && b[2] < d[2];
+    const float wxy[2][2] = {{wt[0][0] * wt[1][0], wt[0][0] * wt[1][1]}, {wt[0][1] * wt[1][0], wt[0][1] * wt[1][1]}};
+    if (inside) {
+        const uint32_t base = uint32_t(b[0]) + fdx * (uint32_t(b[1]) + fdy * uint32_t(b[2]));
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+            t.w[k] = wxy[ox][oy] * wt[2][oz];
+            t.idx[k] = base + uint32_t(ox) + fdx * uint32_t(oy) + fdx * fdy * uint32_t(oz);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+            const int qx = clampi(b[0] + ox, 0, d[0]);
+            const int qy = clampi(b[1] + oy, 0, d[1]);
+            const int qz = clampi(b[2] + oz, 0, d[2]);
+            t.w[k] = wxy[ox][oy] * wt[2][oz];
+            t.idx[k] = uint32_t(qx) + fdx * (uint32_t(qy) + fdy * uint32_t(qz));
+        }
+    }
+}
+
+__device__ __forceinline__ float gather(const float* __restrict__ buf, const Taps& t) {
     float acc = 0.0f;
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
-        const int qx = clampi(b[0] + ox, 0, d[0]);
-        const int qy = clampi(b[1] + oy, 0, d[1]);
-        const int qz = clampi(b[2] + oz, 0, d[2]);
-        const float wgt = wt[0][ox] * wt[1][oy] * wt[2][oz];
-        acc += wgt * __ldg(buf + uint32_t(qx) + fdx * (uint32_t(qy) + fdy * uint32_t(qz)));
-    }
+    for (int k = 0; k < 8; k++) acc += t.w[k] * __ldg(buf + t.idx[k]);
     return acc;
 }
 
@@ -464,16 +496,16 @@ __global__ void __launch_bounds__(256) k_g2p(Work w) {
         if (live) {
             P = s.posB[i];
             V = s.velB[i];
-            const float* fu = s.vel;
-            const float* fv = s.vel + s.nu;
-            const float* fw = s.vel + s.nu + s.nv;
-            const float* ou = s.vel_old;
-            const float* ov = s.vel_old + s.nu;
-            const float* ow = s.vel_old + s.nu + s.nv;
-            const float pic[3] = {sample_face(s, fu, 0, P.x, P.y, P.z), sample_face(s, fv, 1, P.x, P.y, P.z),
-                                  sample_face(s, fw, 2, P.x, P.y, P.z)};
-            const float old[3] = {sample_face(s, ou, 0, P.x, P.y, P.z), sample_face(s, ov, 1, P.x, P.y, P.z),
-                                  sample_face(s, ow, 2, P.x, P.y, P.z)};
+            const float* fvel[3] = {s.vel, s.vel + s.nu, s.vel + s.nu + s.nv};
+            const float* fold[3] = {s.vel_old, s.vel_old + s.nu, s.vel_old + s.nu + s.nv};
+            float pic[3], old[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Taps t;
+                face_taps(s, c, P.x, P.y, P.z, t);
+                pic[c] = gather(fvel[c], t);
+                old[c] = gather(fold[c], t);
+            }
             const float pv[3] = {V.x, V.y, V.z};
             float x[3] = {P.x, P.y, P.z};
             float v[3], mid[3];
@@ -484,9 +516,13 @@ __global__ void __launch_bounds__(256) k_g2p(Work w) {
                 v[a] = fmix(pic[a], fl, s.flip);
                 mid[a] = x[a] + hdt * pic[a];
             }
-            const float sv[3] = {sample_face(s, fu, 0, mid[0], mid[1], mid[2]),
-                                 sample_face(s, fv, 1, mid[0], mid[1], mid[2]),
-                                 sample_face(s, fw, 2, mid[0], mid[1], mid[2])};
+            float sv[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                Taps t;
+                face_taps(s, c, mid[0], mid[1], mid[2], t);
+                sv[c] = gather(fvel[c], t);
+            }
             const int n[3] = {s.nx, s.ny, s.nz};
 #pragma unroll
             for (int a = 0; a < 3; a++) {
