@@ -50,6 +50,9 @@ struct BatchImpl {
     std::vector<pxf_sim*> sims;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;         // body capture of the conditional node
+    cudaStream_t side2 = nullptr;        // body capture of the nested restart IF node
+    bool if_ok = true;                   // nested IF node usable inside the while body
+    bool retried_plain_if = false;
     SimDev* d_sims = nullptr;
     uint32_t* d_base = nullptr;
     size_t cap_sims = 0;
@@ -82,6 +85,7 @@ struct BatchImpl {
     int wait();
     void drop_graphs();
     int profile(pxf_stage_time* out, uint32_t cap, uint32_t* count);
+    cudaError_t capture_restart(cudaStream_t st, int n);
 };
 
 }  // namespace pxf
@@ -134,7 +138,7 @@ struct Layout {
         x2, x64, r, z, p0, p1, Ap, partial, pcg, total;
     int nlev = 0;
     int dims[kMaxLevels][3];
-    size_t ltype[kMaxLevels], linfo[kMaxLevels], lr[kMaxLevels], lz[kMaxLevels];
+    size_t ltype[kMaxLevels], linfo[kMaxLevels], lr[kMaxLevels], lz[kMaxLevels], llist[kMaxLevels], llcnt[kMaxLevels];
 };
 
 // Multigrid hierarchy: halve (rounding up) while the level has more than 512 cells and every
@@ -174,7 +178,7 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
     L.type = take(nc);
     L.count = take(4 * nc);
     L.start = take(4 * (nc + 1));
-    L.chunk = take(4 * nchunks);
+    L.chunk = take(4 * (nchunks + 1));   // + the dense-cell flag of the last binning
     L.info = take(2 * nc);
     L.acc = o.keep_p2g_sums ? take(4 * nf) : 0;
     L.wacc = o.keep_p2g_sums ? take(4 * nf) : 0;
@@ -189,14 +193,19 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
         L.Ap = take(4 * nc);
         L.partial = take(8 * nchunks);
         L.pcg = take(sizeof(PcgState));
+        L.llist[0] = take(4 * nchunks * kScanChunk);
+        L.llcnt[0] = take(8 * nchunks);
         if (o.pcg_precond == 0) {
             L.nlev = mg_levels(n, L.dims);
             for (int l = 1; l < L.nlev; l++) {
                 const uint64_t c = uint64_t(L.dims[l][0]) * L.dims[l][1] * L.dims[l][2];
+                const uint64_t ch = (c + kScanChunk - 1) / kScanChunk;
                 L.ltype[l] = take(c);
                 L.linfo[l] = take(2 * c);
                 L.lr[l] = take(4 * c);
                 L.lz[l] = take(4 * c);
+                L.llist[l] = take(4 * ch * kScanChunk);
+                L.llcnt[l] = take(8 * ch);
             }
         }
     }
@@ -211,6 +220,7 @@ BatchImpl::~BatchImpl() {
     if (d_flag) cudaFree(d_flag);
     if (h_flag) cudaFreeHost(h_flag);
     if (side) cudaStreamDestroy(side);
+    if (side2) cudaStreamDestroy(side2);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -233,6 +243,7 @@ int BatchImpl::rebuild() {
     if (!stream) {
         if ((e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
         if ((e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+        if ((e = cudaStreamCreateWithFlags(&side2, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     }
     drop_graphs();
     const int n = int(sims.size());
@@ -347,6 +358,45 @@ int BatchImpl::record_post(cudaStream_t st) {
     return PXF_OK;
 }
 
+// Inside the captured while body: `if (any simulation needs an FP64 restart) { restart kernels }`
+// as a nested IF node; plain (self-skipping) launches when nesting is unavailable.
+cudaError_t BatchImpl::capture_restart(cudaStream_t st, int n) {
+    if (!if_ok) return launch_pcg_restart(pw, st);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = launch_pcg_restart_cond(d_sims, n, h, st);
+    if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+    alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
+    std::memset(np_raw, 0, sizeof(np_raw));
+    cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_raw);
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e == cudaSuccess) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(side2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e1 = launch_pcg_restart(pw, side2);
+            cudaGraph_t out = body;
+            cudaError_t e2 = cudaStreamEndCapture(side2, &out);
+            e = e1 != cudaSuccess ? e1 : e2;
+        }
+    }
+    if (e != cudaSuccess) if_ok = false;
+    return e;
+}
+
 static cudaError_t end_capture_to_exec(cudaStream_t st, cudaGraphExec_t* exec) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -396,7 +446,10 @@ int BatchImpl::capture() {
                 cudaGraph_t body = np.conditional.phGraph_out[0];
                 e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
-                    cudaError_t e1 = launch_pcg_body(pw, side);
+                    cudaError_t e1 = launch_pcg_dir(pw, side);
+                    if (e1 == cudaSuccess) e1 = launch_pcg_update(pw, side);
+                    if (e1 == cudaSuccess) e1 = capture_restart(side, n);
+                    if (e1 == cudaSuccess) e1 = launch_precond(pw, side);
                     cudaError_t e2 = launch_pcg_cond(d_sims, n, h, side);
                     cudaGraph_t out = body;
                     cudaError_t e3 = cudaStreamEndCapture(side, &out);
@@ -415,6 +468,10 @@ int BatchImpl::capture() {
         if (ex) cudaGraphExecDestroy(ex);
         cudaGetLastError();
         if (rc) return rc;
+        if (!if_ok && !retried_plain_if) {
+            retried_plain_if = true;
+            return capture();   // once more with the restart kernels as plain launches
+        }
         if (!cond_failed && e != cudaSuccess) return cuda_fail(e, "graph instantiate");
         cond_ok = false;   // fall through to the host-driven precision loop
     }
@@ -737,6 +794,8 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
         d.lev[0].info = d.info;
         d.lev[0].r = d.r;
         d.lev[0].z = d.z;
+        d.lev[0].list = reinterpret_cast<uint32_t*>(m + L.llist[0]);
+        d.lev[0].lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[0]);
         for (int l = 1; l < L.nlev; l++) {
             MgLevel& v = d.lev[l];
             v.nx = L.dims[l][0]; v.ny = L.dims[l][1]; v.nz = L.dims[l][2];
@@ -745,6 +804,8 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
             v.info = reinterpret_cast<uint16_t*>(m + L.linfo[l]);
             v.r = reinterpret_cast<float*>(m + L.lr[l]);
             v.z = reinterpret_cast<float*>(m + L.lz[l]);
+            v.list = reinterpret_cast<uint32_t*>(m + L.llist[l]);
+            v.lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[l]);
         }
     }
 

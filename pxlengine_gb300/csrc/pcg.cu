@@ -116,7 +116,68 @@ __device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
     return out;
 }
 
+// Entries [lo, hi) of chunk `chunk` of a level's system-cell list for colour 0 (red), 1 (black)
+// or 2 (both).
+__device__ __forceinline__ void seg(const MgLevel& L, uint32_t chunk, int color, uint32_t& lo, uint32_t& hi) {
+    const uint32_t nr = __ldg(L.lcnt + 2 * chunk), nb = __ldg(L.lcnt + 2 * chunk + 1);
+    lo = color == 1 ? nr : 0u;
+    hi = color == 0 ? nr : nr + nb;
+}
+
 }  // namespace
+
+// ============================================================================ system-cell lists
+// Compacts each 2048-cell chunk of level l into its red then black system cells, in ascending
+// cell order (a block scan, so the order and every reduction over it are deterministic).
+__global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) {
+    __shared__ uint32_t wr[THREADS / 32], wb[THREADS / 32];
+    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev* sp = w.sims + si;
+        if (sp->solver != 1) continue;
+        const MgLevel L = sp->lev[l];
+        const uint32_t chunk = item - w.base[si];
+        const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
+        const uint32_t c0 = chunk * kScanChunk + threadIdx.x * PER_THREAD;
+        uint32_t redm = 0, blkm = 0;
+#pragma unroll
+        for (int k = 0; k < PER_THREAD; k++) {
+            const uint32_t c = c0 + k;
+            if (c >= L.nc || !in_system(L.info[c])) continue;
+            const uint32_t par = (c % nx + (c / nx) % ny + c / nxy) & 1u;
+            if (par) blkm |= 1u << k; else redm |= 1u << k;
+        }
+        const uint32_t nr = __popc(redm), nb = __popc(blkm);
+        // block exclusive scans of nr and nb
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        uint32_t xr = nr, xb = nb;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t yr = __shfl_up_sync(0xffffffffu, xr, d), yb = __shfl_up_sync(0xffffffffu, xb, d);
+            if (lane >= d) { xr += yr; xb += yb; }
+        }
+        if (lane == 31) { wr[wid] = xr; wb[wid] = xb; }
+        __syncthreads();
+        uint32_t br = 0, bb = 0, tr = 0, tb = 0;
+        for (int k = 0; k < THREADS / 32; k++) {
+            if (k < wid) { br += wr[k]; bb += wb[k]; }
+            tr += wr[k];
+            tb += wb[k];
+        }
+        uint32_t pr = br + xr - nr, pb = tr + bb + xb - nb;
+        uint32_t* out = L.list + size_t(chunk) * kScanChunk;
+#pragma unroll
+        for (int k = 0; k < PER_THREAD; k++) {
+            if (redm & (1u << k)) out[pr++] = c0 + k;
+            if (blkm & (1u << k)) out[pb++] = c0 + k;
+        }
+        if (threadIdx.x == 0) {
+            L.lcnt[2 * chunk] = tr;
+            L.lcnt[2 * chunk + 1] = tb;
+        }
+        __syncthreads();
+    }
+}
 
 // ============================================================================ multigrid setup
 // Type of level l+1 from its children on level l.
@@ -194,15 +255,15 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
         const uint32_t chunk = item - w.base[si];
         const MgLevel Cc = (mode == 2) ? sp->lev[l + 1] : L;
         const uint32_t cnx = uint32_t(Cc.nx), cnxy = uint32_t(Cc.nx) * uint32_t(Cc.ny);
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= L.nc) continue;
+        uint32_t lo, hi;
+        seg(L, chunk, color, lo, hi);
+        const uint32_t* lst = L.list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             const uint32_t inf = L.info[c];
-            if (!in_system(inf)) continue;
-            const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
-            if (((i + j + kk) & 1u) != uint32_t(color)) continue;
             float sum = L.r[c];
-            if (mode != 1) {
+            if (mode == 2) {
+                const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
 #pragma unroll
                 for (int q = 0; q < 6; q++) {
                     if (!(inf & (1u << q))) continue;
@@ -211,13 +272,15 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
                     const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
                     const uint32_t n = uint32_t(int64_t(c) + dx + int64_t(dy) * nx + int64_t(dz) * nxy);
                     float zn = L.z[n];
-                    if (mode == 2) {
-                        const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
-                                           cnxy * (uint32_t(int(kk) + dz) >> 1);
-                        if (in_system(Cc.info[P])) zn += Cc.z[P];
-                    }
+                    const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
+                                       cnxy * (uint32_t(int(kk) + dz) >> 1);
+                    if (in_system(Cc.info[P])) zn += Cc.z[P];
                     sum += zn;
                 }
+            } else if (mode != 1) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (inf & (1u << q)) sum += L.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
             }
             L.z[c] = sum / cnt_of(inf);
         }
@@ -225,9 +288,10 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
             // r.z over every system cell of the chunk (the other colour was final before this sweep).
             __syncthreads();
             DF acc{0.f, 0.f};
-            for (int k = 0; k < PER_THREAD; k++) {
-                const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-                if (c >= L.nc || !in_system(L.info[c])) continue;
+            uint32_t a0, a1;
+            seg(L, chunk, 2, a0, a1);
+            for (uint32_t e = a0 + threadIdx.x; e < a1; e += THREADS) {
+                const uint32_t c = lst[e];
                 acc = df_add(acc, two_prod(L.r[c], L.z[c]));
             }
             const double t = block_sum(acc, sh);
@@ -243,27 +307,28 @@ __global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
         const SimDev* sp = w.sims + si;
         if (!active(*sp) || sp->precond != 0) continue;
         const MgLevel F = sp->lev[l], Cc = sp->lev[l + 1];
-        const int64_t nx = F.nx, nxy = int64_t(F.nx) * F.ny;
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t P = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
-            if (P >= Cc.nc) continue;
+        const uint32_t nx = uint32_t(F.nx), nxy = uint32_t(F.nx) * uint32_t(F.ny);
+        const uint32_t chunk = item - w.base[si];
+        uint32_t lo, hi;
+        seg(Cc, chunk, 2, lo, hi);
+        const uint32_t* lst = Cc.list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t P = lst[e];
+            const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
+            const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
             float sum = 0.0f;
-            if (in_system(Cc.info[P])) {
-                const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
-                const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
 #pragma unroll
-                for (int ch = 0; ch < 8; ch++) {
-                    const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
-                    if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
-                    const int64_t c = int64_t(i) + nx * j + nxy * kk;
-                    const uint32_t inf = F.info[c];
-                    if (!in_system(inf)) continue;
-                    float az = cnt_of(inf) * F.z[c];
+            for (int ch = 0; ch < 8; ch++) {
+                const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
+                if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
+                const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
+                const uint32_t inf = F.info[c];
+                if (!in_system(inf)) continue;
+                float az = cnt_of(inf) * F.z[c];
 #pragma unroll
-                    for (int q = 0; q < 6; q++)
-                        if (inf & (1u << q)) az -= F.z[c + nbr(q, nx, nxy)];
-                    sum += F.r[c] - az;
-                }
+                for (int q = 0; q < 6; q++)
+                    if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+                sum += F.r[c] - az;
             }
             Cc.r[P] = 0.5f * sum;
         }
@@ -419,11 +484,12 @@ __global__ void __launch_bounds__(THREADS) k_jacobi(Work w) {
         if (!active(s) || s.precond != 1) continue;
         const uint32_t chunk = item - w.base[si];
         DF acc{0.f, 0.f};
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc) continue;
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
-            if (!in_system(inf)) continue;
             const float r = s.r[c];
             const float z = r / cnt_of(inf);
             s.z[c] = z;
@@ -444,9 +510,11 @@ __global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) {
         if (s.solver != 1) continue;
         const uint32_t chunk = item - w.base[si];
         DF acc{0.f, 0.f};
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc || !in_system(s.info[c])) continue;
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             const float b = rhs_of(s, c);
             acc = df_add(acc, two_prod(b, b));
         }
@@ -462,9 +530,12 @@ __global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) {
         const SimDev s = w.sims[si];
         if (!active(s) || !ldu(&s.pcg->restart_now)) continue;
         const bool zero = ldu(&s.pcg->zero_x) != 0;
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc || !in_system(s.info[c])) continue;
+        const uint32_t chunk = item - w.base[si];
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             if (zero) {
                 s.x2[c] = make_float2(0.f, 0.f);
                 s.x64[c] = 0.0;
@@ -486,11 +557,12 @@ __global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) {
         const uint32_t chunk = item - w.base[si];
         const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         double rr = 0;
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc) continue;
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
-            if (!in_system(inf)) continue;
             double ax = double(cnt_of(inf)) * s.x64[c];
 #pragma unroll
             for (int q = 0; q < 6; q++)
@@ -529,11 +601,12 @@ __global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) {
         const float beta = float(ldd(&st->beta));
         const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         DF acc{0.f, 0.f};
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc) continue;
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
-            if (!in_system(inf)) continue;
             const float pn = fresh ? s.z[c] : s.z[c] + beta * pold[c];
             float ap = cnt_of(inf) * pn;
 #pragma unroll
@@ -565,9 +638,11 @@ __global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) {
         const float ah = ldf(&st->alpha_hi), al = ldf(&st->alpha_lo);
         const float af = float(ldd(&st->alpha));
         DF acc{0.f, 0.f};
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = chunk * kScanChunk + k * THREADS + threadIdx.x;
-            if (c >= s.nc || !in_system(s.info[c])) continue;
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+            const uint32_t c = lst[e];
             const float pc = p[c];
             DF d = two_prod(ah, pc);
             d.lo += al * pc;
@@ -690,6 +765,16 @@ __global__ void k_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalH
     cudaGraphSetConditional(h, any);
 }
 
+__global__ void k_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned any = 0;
+    for (int i = 0; i < n_sims; i++) {
+        const SimDev& s = sims[i];
+        if (s.solver == 1 && !__ldcg(&s.pcg->done) && __ldcg(&s.pcg->restart_now)) any = 1;
+    }
+    cudaGraphSetConditional(h, any);
+}
+
 __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     uint32_t any = 0;
@@ -725,10 +810,12 @@ cudaError_t mg_tail_attr(size_t smem) {
 }
 
 cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
+    k_cell_lists<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks), 0);
     for (int l = 0; l + 1 < pw.setup_levels; l++) {
         if (!pw.setup[l].total) continue;
         k_mg_coarsen<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l);
         k_mg_info<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l);
+        k_cell_lists<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l + 1);
     }
     return cudaGetLastError();
 }
@@ -781,6 +868,11 @@ cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st) {
     launch_pcg_update(pw, st);
     launch_pcg_restart(pw, st);
     return launch_precond(pw, st);
+}
+
+cudaError_t launch_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {
+    k_pcg_restart_cond<<<1, 32, 0, st>>>(sims, n_sims, h);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {

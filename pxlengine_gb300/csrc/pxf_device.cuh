@@ -47,6 +47,10 @@ struct MgLevel {
     uint16_t* info;
     float* r;
     float* z;
+    // System cells of each 2048-cell chunk, in ascending order: chunk k owns list[2048 k ...],
+    // first its red cells ((i + j + k) even), then its black cells; lcnt[2k], lcnt[2k+1] count them.
+    uint32_t* list;
+    uint32_t* lcnt;
 };
 constexpr int kMaxLevels = 12;
 

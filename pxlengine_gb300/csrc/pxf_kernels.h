@@ -64,6 +64,8 @@ cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
+// Sets an IF condition: does any simulation need an FP64 restart residual now?
+cudaError_t launch_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
 // Host-driven fallback: a flag telling whether any simulation still runs.
 cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaStream_t st);
 

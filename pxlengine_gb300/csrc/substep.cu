@@ -20,6 +20,13 @@ namespace pxf {
 
 constexpr uint32_t SCAN_CHUNK = 2048;   // cells per scan work item (256 threads x 8)
 
+// P2G packs a face's two int32 sums into one 64-bit shared atomic: acc in the high word, wacc in
+// the low word. Every wacc term is int(w * 65536) with 0 <= w <= 1 and a face collects terms from
+// the particles of 18 cells, so with at most 3640 particles per cell (18 * 3640 * 65536 < 2^32) the
+// low word never carries into the high word and both words equal the reference's wrapping int32
+// sums. Binnings with a denser cell use two 32-bit atomics instead.
+constexpr uint32_t kPackedMaxPerCell = 3640;
+
 // ------------------------------------------------------------------ counting sort: scan + classify
 // Per-chunk sums of the per-cell particle counts.
 __global__ void __launch_bounds__(256) k_scan_chunks(Work w) {
@@ -54,7 +61,10 @@ __global__ void __launch_bounds__(1024) k_scan_sims(const SimDev* sims, int n_si
     for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
         const SimDev s = sims[si];
         const uint32_t nchunks = (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK;
-        if (threadIdx.x == 0) carry = 0;
+        if (threadIdx.x == 0) {
+            carry = 0;
+            s.chunk[nchunks] = 0;   // dense-cell flag of this binning (raised by k_scan_apply)
+        }
         __syncthreads();
         for (uint32_t base = 0; base < nchunks; base += 1024) {
             const uint32_t i = base + threadIdx.x;
@@ -126,6 +136,7 @@ __global__ void __launch_bounds__(256) k_scan_apply(Work w) {
                 s.start[c] = before;
                 before += v[k];
                 s.count[c] = 0;
+                if (v[k] > kPackedMaxPerCell) atomicOr(&s.chunk[(s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK], 1u);
                 const int i = int(c % uint32_t(s.nx));
                 const int j = int((c / uint32_t(s.nx)) % uint32_t(s.ny));
                 const int kk = int(c / nxy);
@@ -205,13 +216,86 @@ struct P2GTile {
     static constexpr int SMEM = NF * 2 * 4;
 };
 
+template <int TX, int TY, int TZ, bool PACKED>
+__device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc, int* __restrict__ swac,
+                                         unsigned long long* __restrict__ spk, const int org[3], const int E[3][3]) {
+    using T = P2GTile<TX, TY, TZ>;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = org[0], y0 = org[1], z0 = org[2];
+    const int sbase[3] = {0, T::FU, T::FU + T::FV};
+    const float SW = 65536.0f;
+    const int rows_y = TY + 2;
+    const int nrows = (TY + 2) * (TZ + 2);
+    for (int r = warp; r < nrows; r += blockDim.x >> 5) {
+        const int yy = y0 - 1 + r % rows_y, zz = z0 - 1 + r / rows_y;
+        if (yy < 0 || yy >= s.ny || zz < 0 || zz >= s.nz) continue;
+        const int xa = max(x0 - 1, 0), xb = min(x0 + TX, s.nx - 1);
+        const uint32_t rowc = uint32_t(s.nx) * (uint32_t(yy) + uint32_t(s.ny) * uint32_t(zz));
+        const uint32_t pb = s.start[rowc + xa], pe = s.start[rowc + xb + 1];
+        // Each lane takes a contiguous slice of the row, so at any step the lanes of a warp sit
+        // in different cells and rarely hit the same face.
+        const uint32_t per = (pe - pb + 31) / 32;
+        for (uint32_t t = 0; t < per; t++) {
+            const uint32_t j = pb + lane * per + t;
+            if (j >= pe) continue;
+            const float4 P = s.posB[j];
+            const float4 V = s.velB[j];
+            const float x[3] = {P.x, P.y, P.z};
+            const float vv[3] = {V.x, V.y, V.z};
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                // Box of this component's owned faces: SDX x SDY x (TZ + (c == 2)) in shared memory.
+                const int SDX = c == 0 ? TX + 1 : TX;
+                const int SDY = c == 1 ? TY + 1 : TY;
+                int lb[3];
+                float wt[3][2];
+                bool ok[3][2];
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    float gq = (x[a] - s.o[a]) * s.inv_h - 0.5f;
+                    if (a == c) gq += 0.5f;
+                    const int b = f2i(floorf(gq));
+                    const float f = gq - float(b);
+                    wt[a][0] = fmix(1.0f - f, f, 0.0f);
+                    wt[a][1] = fmix(1.0f - f, f, 1.0f);
+                    lb[a] = b - org[a];
+                    ok[a][0] = unsigned(lb[a]) < unsigned(E[c][a]);
+                    ok[a][1] = unsigned(lb[a] + 1) < unsigned(E[c][a]);
+                }
+                if (!((ok[0][0] | ok[0][1]) & (ok[1][0] | ok[1][1]) & (ok[2][0] | ok[2][1]))) continue;
+                // w = (wx * wy) * wz, the reference's product order
+                const float wxy[2][2] = {{wt[0][0] * wt[1][0], wt[0][0] * wt[1][1]},
+                                         {wt[0][1] * wt[1][0], wt[0][1] * wt[1][1]}};
+                const int base = sbase[c] + lb[0] + SDX * (lb[1] + SDY * lb[2]);
+                const float v = vv[c];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+                    if (!(ok[0][ox] & ok[1][oy] & ok[2][oz])) continue;
+                    const float wgt = wxy[ox][oy] * wt[2][oz];
+                    const int idx = base + ox + SDX * oy + SDX * SDY * oz;
+                    const int ta = f2i(wgt * v * SW);
+                    const int tw = f2i(wgt * SW);
+                    if (PACKED) {
+                        atomicAdd(&spk[idx], (static_cast<unsigned long long>(static_cast<uint32_t>(ta)) << 32) |
+                                                 static_cast<uint32_t>(tw));
+                    } else {
+                        atomicAdd(&sacc[idx], ta);
+                        atomicAdd(&swac[idx], tw);
+                    }
+                }
+            }
+        }
+    }
+}
+
 template <int TX, int TY, int TZ>
 __global__ void __launch_bounds__(256) k_p2g(Work w) {
     using T = P2GTile<TX, TY, TZ>;
-    extern __shared__ int smem[];
-    int* sacc = smem;
-    int* swac = smem + T::NF;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    extern __shared__ unsigned long long smem64[];
+    unsigned long long* spk = smem64;
+    int* sacc = reinterpret_cast<int*>(smem64);
+    int* swac = sacc + T::NF;
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -236,61 +320,11 @@ __global__ void __launch_bounds__(256) k_p2g(Work w) {
         const int sbase[3] = {0, T::FU, T::FU + T::FV};
         const int sdx[3] = {TX + 1, TX, TX};
         const int sdy[3] = {TY, TY + 1, TY};
-        for (int i = threadIdx.x; i < T::NF; i += blockDim.x) { sacc[i] = 0; swac[i] = 0; }
+        const bool packed = __ldg(s.chunk + (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK) == 0;
+        for (int i = threadIdx.x; i < T::NF; i += blockDim.x) spk[i] = 0ull;   // also zeroes sacc / swac
         __syncthreads();
-
-        const float SW = 65536.0f;
-        const int rows_y = TY + 2;
-        const int nrows = (TY + 2) * (TZ + 2);
-        for (int r = warp; r < nrows; r += blockDim.x >> 5) {
-            const int yy = y0 - 1 + r % rows_y, zz = z0 - 1 + r / rows_y;
-            if (yy < 0 || yy >= s.ny || zz < 0 || zz >= s.nz) continue;
-            const int xa = max(x0 - 1, 0), xb = min(x0 + TX, s.nx - 1);
-            const uint32_t rowc = uint32_t(s.nx) * (uint32_t(yy) + uint32_t(s.ny) * uint32_t(zz));
-            const uint32_t pb = s.start[rowc + xa], pe = s.start[rowc + xb + 1];
-            for (uint32_t j = pb + lane; j < pe; j += 32) {
-                const float4 P = s.posB[j];
-                const float4 V = s.velB[j];
-                const float x[3] = {P.x, P.y, P.z};
-                const float vv[3] = {V.x, V.y, V.z};
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    // Box of this component's owned faces: SDX x SDY x (TZ + (c == 2)) in shared memory.
-                    const int SDX = c == 0 ? TX + 1 : TX;
-                    const int SDY = c == 1 ? TY + 1 : TY;
-                    int lb[3];
-                    float wt[3][2];
-                    bool ok[3][2];
-#pragma unroll
-                    for (int a = 0; a < 3; a++) {
-                        float gq = (x[a] - s.o[a]) * s.inv_h - 0.5f;
-                        if (a == c) gq += 0.5f;
-                        const int b = f2i(floorf(gq));
-                        const float f = gq - float(b);
-                        wt[a][0] = fmix(1.0f - f, f, 0.0f);
-                        wt[a][1] = fmix(1.0f - f, f, 1.0f);
-                        lb[a] = b - org[a];
-                        ok[a][0] = unsigned(lb[a]) < unsigned(E[c][a]);
-                        ok[a][1] = unsigned(lb[a] + 1) < unsigned(E[c][a]);
-                    }
-                    if (!((ok[0][0] | ok[0][1]) & (ok[1][0] | ok[1][1]) & (ok[2][0] | ok[2][1]))) continue;
-                    // w = (wx * wy) * wz, the reference's product order
-                    const float wxy[2][2] = {{wt[0][0] * wt[1][0], wt[0][0] * wt[1][1]},
-                                             {wt[0][1] * wt[1][0], wt[0][1] * wt[1][1]}};
-                    const int base = sbase[c] + lb[0] + SDX * (lb[1] + SDY * lb[2]);
-                    const float v = vv[c];
-#pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        const int ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
-                        if (!(ok[0][ox] & ok[1][oy] & ok[2][oz])) continue;
-                        const float wgt = wxy[ox][oy] * wt[2][oz];
-                        const int idx = base + ox + SDX * oy + SDX * SDY * oz;
-                        atomicAdd(&sacc[idx], f2i(wgt * v * SW));
-                        atomicAdd(&swac[idx], f2i(wgt * SW));
-                    }
-                }
-            }
-        }
+        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E);
+        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E);
         __syncthreads();
 
         // Epilogue: normalize + forces for the owned faces.
@@ -304,7 +338,15 @@ __global__ void __launch_bounds__(256) k_p2g(Work w) {
             for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
                 const int lx = idx % ex, ly = (idx / ex) % ey, lz = idx / (ex * ey);
                 const int si2 = sbase[c] + lx + sdx[c] * (ly + sdy[c] * lz);
-                const int a = sacc[si2], wv = swac[si2];
+                int a, wv;
+                if (packed) {
+                    const unsigned long long pk = spk[si2];
+                    a = static_cast<int>(static_cast<uint32_t>(pk >> 32));
+                    wv = static_cast<int>(static_cast<uint32_t>(pk));
+                } else {
+                    a = sacc[si2];
+                    wv = swac[si2];
+                }
                 const float v = wv > 0 ? float(a) / float(wv) : 0.0f;
                 const int fx = x0 + lx, fy = y0 + ly, fz = z0 + lz;
                 const uint32_t fi = fbase + uint32_t(fx) + fdx * (uint32_t(fy) + fdy * uint32_t(fz));

@@ -72,10 +72,12 @@ def test_thirty_substeps_bit_exact(lib):
         particles_equal(s, o)
 
 
-def test_random_particles_and_edges(lib):
+@pytest.mark.parametrize("pile", [300, 5000])
+def test_random_particles_and_edges(lib, pile):
     """Arbitrary particle states: jittered positions, exact cell-boundary positions, a pile of
-    particles in one cell, velocities of both signs and magnitudes."""
-    f = dam(res=24, ppc=2)
+    particles in one cell (5000 exceeds the packed P2G accumulation's per-cell bound and takes
+    the two-atomic path), velocities of both signs and magnitudes."""
+    f = dam(res=24, ppc=2) if pile < 1000 else dam(res=32, ppc=8)
     with P.FluidState(f, fps=24.0, seed=1, options=P.make_options(keep_p2g_sums=True)) as s:
         n = s.particle_count()
         nx, ny, nz = s.dims
@@ -87,7 +89,7 @@ def test_random_particles_and_edges(lib):
         p[:, :3] = (lo + rng.random((n, 3), dtype=np.float32) * (hi - lo)).astype(np.float32)
         k = n // 4
         p[:k, :3] = (rng.integers(1, [nx - 1, ny - 1, nz - 1], size=(k, 3)).astype(np.float32) * h)
-        p[k:k + 300, :3] = np.float32(5.5) * h            # 300 particles in one cell
+        p[k:k + pile, :3] = np.float32(5.5) * h           # a pile of particles in one cell
         p[:, 4:7] = rng.normal(0, 2.0, (n, 3)).astype(np.float32)
         p[:50, 4:7] *= np.float32(50.0)
         s.write_particles(p)
