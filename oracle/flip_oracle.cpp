@@ -64,7 +64,7 @@ template <class T> struct Sim {
     // FP64 dot products, FP64 solution and FP64 restart residuals, 2 = Jacobi-PCG entirely in FP64,
     // 3 = as 1 with a multigrid V-cycle preconditioner in FP32 (the CUDA precision solver).
     int pmode = 0;
-    uint32_t mg_coarse_iters = 16;   // symmetric red-black iterations on the coarsest level
+    uint32_t mg_coarse_iters = 2;    // symmetric red-black iterations on the coarsest level
     double rtol = 1e-6;
     uint32_t max_iter = 2000, restart = 50;
     uint32_t last_iters = 0;
@@ -314,7 +314,7 @@ template <class T> struct Sim {
     // black, red), restriction sums the children's residuals times 1/2 and prolongation injects
     // the coarse correction into every child, so restriction = prolongation^T / 2 and the cycle
     // is a symmetric operator. The coarsest level (<= 512 cells) runs mg_coarse_iters
-    // red-black iterations followed by as many black-red iterations from zero.
+    // (default 2) red-black iterations followed by as many black-red iterations from zero.
     struct Level {
         int nx = 0, ny = 0, nz = 0;
         std::vector<uint8_t> type, fmask, cnt;
@@ -818,6 +818,12 @@ int orc_sim_set_pressure(void* p, int mode, double rtol, uint32_t max_iter, uint
     auto* hd = static_cast<Handle*>(p);
     auto set = [&](auto* s) { s->pmode = mode; s->rtol = rtol; s->max_iter = max_iter; s->restart = restart ? restart : 50; };
     if (hd->dbl) set(hd->d); else set(hd->f);
+    return 0;
+}
+
+int orc_sim_set_mg(void* p, uint32_t coarse_iters) {
+    auto* hd = static_cast<Handle*>(p);
+    if (hd->dbl) hd->d->mg_coarse_iters = coarse_iters; else hd->f->mg_coarse_iters = coarse_iters;
     return 0;
 }
 

@@ -748,7 +748,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.max_iter = opts.pcg_max_iter;
     d.restart = opts.pcg_restart ? opts.pcg_restart : 50;
     d.precond = opts.pcg_precond;
-    d.coarse_iters = opts.mg_coarse_iters ? opts.mg_coarse_iters : 16;
+    d.coarse_iters = opts.mg_coarse_iters ? opts.mg_coarse_iters : 2;
 
     cudaError_t e = cudaMalloc(&s->mem, L.total);
     if (e != cudaSuccess) {
@@ -872,7 +872,7 @@ void pxf_options_init(pxf_options* o) {
     o->wait_timeout_s = 600.0;
     o->p2g_tile = -1;
     o->pcg_precond = 0;
-    o->mg_coarse_iters = 16;
+    o->mg_coarse_iters = 2;
 }
 
 int pxf_validate(const pxf_fluid_desc* desc, uint32_t index, uint32_t lift, char* msg, size_t cap) {

@@ -312,25 +312,34 @@ __global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
         uint32_t lo, hi;
         seg(Cc, chunk, 2, lo, hi);
         const uint32_t* lst = Cc.list + size_t(chunk) * kScanChunk;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
-            const uint32_t P = lst[e];
-            const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
-            const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
-            float sum = 0.0f;
+        // 8 consecutive lanes per coarse cell, one child each.
+        const uint32_t chd = threadIdx.x & 7u;
+        for (uint32_t base = lo; base < hi; base += THREADS / 8) {
+            const uint32_t e = base + (threadIdx.x >> 3);
+            float res = 0.0f;
+            uint32_t P = 0;
+            if (e < hi) {
+                P = lst[e];
+                const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
+                const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
+                const int i = 2 * I + int(chd & 1u), j = 2 * J + int((chd >> 1) & 1u), kk = 2 * K + int(chd >> 2);
+                if (i < F.nx && j < F.ny && kk < F.nz) {
+                    const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
+                    const uint32_t inf = F.info[c];
+                    if (in_system(inf)) {
+                        float az = cnt_of(inf) * F.z[c];
 #pragma unroll
-            for (int ch = 0; ch < 8; ch++) {
-                const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
-                if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
-                const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
-                const uint32_t inf = F.info[c];
-                if (!in_system(inf)) continue;
-                float az = cnt_of(inf) * F.z[c];
-#pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
-                sum += F.r[c] - az;
+                        for (int q = 0; q < 6; q++)
+                            if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+                        res = F.r[c] - az;
+                    }
+                }
             }
-            Cc.r[P] = 0.5f * sum;
+            // ((c0 + c1) + (c2 + c3)) + ((c4 + c5) + (c6 + c7))
+            res += __shfl_down_sync(0xffffffffu, res, 1, 8);
+            res += __shfl_down_sync(0xffffffffu, res, 2, 8);
+            res += __shfl_down_sync(0xffffffffu, res, 4, 8);
+            if (e < hi && chd == 0) Cc.r[P] = 0.5f * res;
         }
     }
 }
@@ -348,46 +357,58 @@ struct TailLevel {
     uint16_t* info;
 };
 
-__device__ void tail_smooth(const TailLevel& L, uint32_t color, int mode, const TailLevel* C) {
+__device__ void tail_smooth(const TailLevel& L, const MgLevel& G, uint32_t color, int mode, const TailLevel* C) {
     const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
-    for (uint32_t c = threadIdx.x; c < L.nc; c += blockDim.x) {
-        const uint32_t inf = L.info[c];
-        if (!in_system(inf)) continue;
-        const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
-        if (((i + j + kk) & 1u) != color) continue;
-        float sum = L.r[c];
-        if (mode != 1) {
+    const uint32_t nch = (L.nc + kScanChunk - 1) / kScanChunk;
+    for (uint32_t ch = 0; ch < nch; ch++) {
+        uint32_t lo, hi;
+        seg(G, ch, int(color), lo, hi);
+        const uint32_t* lst = G.list + size_t(ch) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+            const uint32_t c = __ldg(lst + e);
+            const uint32_t inf = L.info[c];
+            float sum = L.r[c];
+            if (mode == 2) {
+                const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
 #pragma unroll
-            for (int q = 0; q < 6; q++) {
-                if (!(inf & (1u << q))) continue;
-                const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
-                const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
-                const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
-                const uint32_t n = uint32_t(int(c) + dx + dy * int(nx) + dz * int(nxy));
-                float zn = L.z[n];
-                if (mode == 2) {
+                for (int q = 0; q < 6; q++) {
+                    if (!(inf & (1u << q))) continue;
+                    const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                    const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                    const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                    const uint32_t n = uint32_t(int(c) + dx + dy * int(nx) + dz * int(nxy));
+                    float zn = L.z[n];
                     const uint32_t P = (uint32_t(int(i) + dx) >> 1) + uint32_t(C->nx) * ((uint32_t(int(j) + dy) >> 1) +
                                        uint32_t(C->ny) * (uint32_t(int(kk) + dz) >> 1));
                     if (in_system(C->info[P])) zn += C->z[P];
+                    sum += zn;
                 }
-                sum += zn;
+            } else if (mode != 1) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (inf & (1u << q)) sum += L.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
             }
+            L.z[c] = sum / cnt_of(inf);
         }
-        L.z[c] = sum / cnt_of(inf);
     }
     __syncthreads();
 }
 
-__device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc) {
+__device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc, const MgLevel& GC) {
     const uint32_t nx = uint32_t(F.nx), nxy = uint32_t(F.nx) * uint32_t(F.ny);
-    for (uint32_t P = threadIdx.x; P < Cc.nc; P += blockDim.x) {
-        float sum = 0.0f;
-        if (in_system(Cc.info[P])) {
+    const uint32_t nch = (Cc.nc + kScanChunk - 1) / kScanChunk;
+    for (uint32_t ch = 0; ch < nch; ch++) {
+        uint32_t lo, hi;
+        seg(GC, ch, 2, lo, hi);
+        const uint32_t* lst = GC.list + size_t(ch) * kScanChunk;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+            const uint32_t P = __ldg(lst + e);
             const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
             const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
+            float sum = 0.0f;
 #pragma unroll
-            for (int ch = 0; ch < 8; ch++) {
-                const int i = 2 * I + (ch & 1), j = 2 * J + ((ch >> 1) & 1), kk = 2 * K + (ch >> 2);
+            for (int chd = 0; chd < 8; chd++) {
+                const int i = 2 * I + (chd & 1), j = 2 * J + ((chd >> 1) & 1), kk = 2 * K + (chd >> 2);
                 if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
                 const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
                 const uint32_t inf = F.info[c];
@@ -398,8 +419,8 @@ __device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc) {
                     if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
                 sum += F.r[c] - az;
             }
+            Cc.r[P] = 0.5f * sum;
         }
-        Cc.r[P] = 0.5f * sum;
     }
     __syncthreads();
 }
@@ -429,21 +450,22 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims
         }
         __syncthreads();
         for (int l = T; l + 1 < NL; l++) {
-            tail_smooth(lv[l], 0, 1, nullptr);
-            tail_smooth(lv[l], 1, 0, nullptr);
-            tail_restrict(lv[l], lv[l + 1]);
+            tail_smooth(lv[l], sp->lev[l], 0, 1, nullptr);
+            tail_smooth(lv[l], sp->lev[l], 1, 0, nullptr);
+            tail_restrict(lv[l], lv[l + 1], sp->lev[l + 1]);
         }
         {
             const TailLevel& Lc = lv[NL - 1];
+            const MgLevel Gc = sp->lev[NL - 1];
             for (uint32_t c = threadIdx.x; c < Lc.nc; c += blockDim.x) Lc.z[c] = 0.0f;
             __syncthreads();
             const uint32_t it = sp->coarse_iters;
-            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, 0, 0, nullptr); tail_smooth(Lc, 1, 0, nullptr); }
-            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, 1, 0, nullptr); tail_smooth(Lc, 0, 0, nullptr); }
+            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, Gc, 0, 0, nullptr); tail_smooth(Lc, Gc, 1, 0, nullptr); }
+            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, Gc, 1, 0, nullptr); tail_smooth(Lc, Gc, 0, 0, nullptr); }
         }
         for (int l = NL - 2; l >= T; l--) {
-            tail_smooth(lv[l], 1, 2, &lv[l + 1]);
-            tail_smooth(lv[l], 0, 0, nullptr);
+            tail_smooth(lv[l], sp->lev[l], 1, 2, &lv[l + 1]);
+            tail_smooth(lv[l], sp->lev[l], 0, 0, nullptr);
         }
         {
             const MgLevel g = sp->lev[T];
@@ -595,29 +617,34 @@ __global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) {
         const uint32_t chunk = item - w.base[si];
         const PcgState* st = s.pcg;
         const uint32_t pbuf = ldu(&st->pbuf);
-        const float* pold = pbuf ? s.p1 : s.p0;
-        float* pnew = pbuf ? s.p0 : s.p1;
+        const float* __restrict__ pold = pbuf ? s.p1 : s.p0;
+        float* __restrict__ pnew = pbuf ? s.p0 : s.p1;
+        const float* __restrict__ z = s.z;
+        float* __restrict__ Ap = s.Ap;
+        const uint16_t* __restrict__ info = s.info;
         const bool fresh = ldu(&st->fresh) != 0;
-        const float beta = float(ldd(&st->beta));
+        const float beta = fresh ? 0.0f : float(ldd(&st->beta));
         const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        const uint32_t* __restrict__ lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+#pragma unroll 2
         for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
             const uint32_t c = lst[e];
-            const uint32_t inf = s.info[c];
-            const float pn = fresh ? s.z[c] : s.z[c] + beta * pold[c];
+            const uint32_t inf = info[c];
+            // p' = z (fresh) or z + beta p: with beta = 0 the fresh case reads pold but ignores it
+            const float pn = fresh ? z[c] : z[c] + beta * pold[c];
             float ap = cnt_of(inf) * pn;
 #pragma unroll
             for (int q = 0; q < 6; q++) {
                 if (inf & (1u << q)) {
                     const int64_t n = int64_t(c) + nbr(q, nx, nxy);
-                    ap -= fresh ? s.z[n] : s.z[n] + beta * pold[n];
+                    ap -= fresh ? z[n] : z[n] + beta * pold[n];
                 }
             }
             pnew[c] = pn;
-            s.Ap[c] = ap;
+            Ap[c] = ap;
             acc = df_add(acc, two_prod(pn, ap));
         }
         const double t = block_sum(acc, sh);
@@ -634,23 +661,27 @@ __global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) {
         if (!active(s)) continue;
         const uint32_t chunk = item - w.base[si];
         const PcgState* st = s.pcg;
-        const float* p = ldu(&st->pbuf) ? s.p1 : s.p0;
+        const float* __restrict__ p = ldu(&st->pbuf) ? s.p1 : s.p0;
+        float2* __restrict__ x2 = s.x2;
+        float* __restrict__ r = s.r;
+        const float* __restrict__ Ap = s.Ap;
         const float ah = ldf(&st->alpha_hi), al = ldf(&st->alpha_lo);
         const float af = float(ldd(&st->alpha));
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        const uint32_t* __restrict__ lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+#pragma unroll 2
         for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
             const uint32_t c = lst[e];
             const float pc = p[c];
             DF d = two_prod(ah, pc);
             d.lo += al * pc;
-            const float2 x = s.x2[c];
+            const float2 x = x2[c];
             const DF xn = df_add(DF{x.x, x.y}, d);
-            s.x2[c] = make_float2(xn.hi, xn.lo);
-            const float rn = s.r[c] - af * s.Ap[c];
-            s.r[c] = rn;
+            x2[c] = make_float2(xn.hi, xn.lo);
+            const float rn = r[c] - af * Ap[c];
+            r[c] = rn;
             acc = df_add(acc, two_prod(rn, rn));
         }
         const double t = block_sum(acc, sh);
@@ -787,7 +818,7 @@ __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
 
 // ============================================================================ launchers
 static unsigned grid_of(uint32_t total) {
-    const uint32_t cap = uint32_t(sm_count() * 8);
+    const uint32_t cap = uint32_t(sm_count() * grid_cap_per_sm());
     return total < cap ? (total ? total : 1u) : cap;
 }
 

@@ -20,6 +20,7 @@ constexpr uint32_t kElemItem = 256;       // elements per item of the per-elemen
 constexpr int kMaxLevelsK = 12;           // multigrid levels (kMaxLevels in pxf_device.cuh)
 
 int sm_count();
+int grid_cap_per_sm();
 void p2g_shape(int shape, int out[3]);
 extern const int kNumP2GShapes;
 

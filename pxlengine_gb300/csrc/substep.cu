@@ -16,6 +16,8 @@
 #include "pxf_device.cuh"
 #include "pxf_kernels.h"
 
+#include <cstdlib>
+
 namespace pxf {
 
 constexpr uint32_t SCAN_CHUNK = 2048;   // cells per scan work item (256 threads x 8)
@@ -218,7 +220,8 @@ struct P2GTile {
 
 template <int TX, int TY, int TZ, bool PACKED>
 __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc, int* __restrict__ swac,
-                                         unsigned long long* __restrict__ spk, const int org[3], const int E[3][3]) {
+                                         unsigned long long* __restrict__ spk, const int org[3], const int E[3][3],
+                                         bool strided) {
     using T = P2GTile<TX, TY, TZ>;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int x0 = org[0], y0 = org[1], z0 = org[2];
@@ -232,11 +235,12 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
         const int xa = max(x0 - 1, 0), xb = min(x0 + TX, s.nx - 1);
         const uint32_t rowc = uint32_t(s.nx) * (uint32_t(yy) + uint32_t(s.ny) * uint32_t(zz));
         const uint32_t pb = s.start[rowc + xa], pe = s.start[rowc + xb + 1];
-        // Each lane takes a contiguous slice of the row, so at any step the lanes of a warp sit
-        // in different cells and rarely hit the same face.
+        // strided: each lane takes a contiguous slice of the row, so at any step the lanes of a
+        // warp sit in different cells and rarely hit the same face; otherwise lanes take
+        // consecutive particles (coalesced loads).
         const uint32_t per = (pe - pb + 31) / 32;
         for (uint32_t t = 0; t < per; t++) {
-            const uint32_t j = pb + lane * per + t;
+            const uint32_t j = strided ? pb + lane * per + t : pb + t * 32 + lane;
             if (j >= pe) continue;
             const float4 P = s.posB[j];
             const float4 V = s.velB[j];
@@ -290,7 +294,7 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
 }
 
 template <int TX, int TY, int TZ>
-__global__ void __launch_bounds__(256) k_p2g(Work w) {
+__global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack) {
     using T = P2GTile<TX, TY, TZ>;
     extern __shared__ unsigned long long smem64[];
     unsigned long long* spk = smem64;
@@ -320,11 +324,11 @@ __global__ void __launch_bounds__(256) k_p2g(Work w) {
         const int sbase[3] = {0, T::FU, T::FU + T::FV};
         const int sdx[3] = {TX + 1, TX, TX};
         const int sdy[3] = {TY, TY + 1, TY};
-        const bool packed = __ldg(s.chunk + (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK) == 0;
+        const bool packed = pack && __ldg(s.chunk + (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK) == 0;
         for (int i = threadIdx.x; i < T::NF; i += blockDim.x) spk[i] = 0ull;   // also zeroes sacc / swac
         __syncthreads();
-        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E);
-        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E);
+        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E, strided != 0);
+        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E, strided != 0);
         __syncthreads();
 
         // Epilogue: normalize + forces for the owned faces.
@@ -638,7 +642,15 @@ int sm_count() {
     return g_sm_count;
 }
 
+// Blocks per launch: every item its own block up to the cap (PXF_GRID_CAP blocks per SM,
+// default 8), beyond which blocks loop over items.
+int grid_cap_per_sm() {
+    static const int cap = [] { const char* v = std::getenv("PXF_GRID_CAP"); int c = v ? std::atoi(v) : 8; return c > 0 ? c : 8; }();
+    return cap;
+}
+
 static unsigned grid_for(uint32_t total, int per_sm) {
+    if (per_sm == 8) per_sm = grid_cap_per_sm();
     const uint32_t cap = uint32_t(sm_count() * per_sm);
     return total < cap ? (total ? total : 1u) : cap;
 }
@@ -664,7 +676,9 @@ static cudaError_t launch_p2g_t(const StageWork& sw, cudaStream_t st) {
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_p2g<TX, TY, TZ>, 256, T::SMEM);
     if (per_sm < 1) per_sm = 1;
-    k_p2g<TX, TY, TZ><<<grid_for(sw.total, per_sm), 256, T::SMEM, st>>>(mk(sw));
+    static const int strided = [] { const char* v = std::getenv("PXF_P2G_STRIDED"); return v ? std::atoi(v) : 1; }();
+    static const int pack = [] { const char* v = std::getenv("PXF_P2G_PACKED"); return v ? std::atoi(v) : 0; }();
+    k_p2g<TX, TY, TZ><<<grid_for(sw.total, per_sm), 256, T::SMEM, st>>>(mk(sw), strided, pack);
     return cudaGetLastError();
 }
 
