@@ -52,6 +52,7 @@ struct BatchImpl {
     cudaStream_t side = nullptr;         // body capture of the conditional node
     cudaStream_t side2 = nullptr;        // body capture of the nested restart IF node
     bool if_ok = true;                   // nested IF node usable inside the while body
+    bool persistent = false;             // the captured substep uses the persistent solve
     bool retried_plain_if = false;
     SimDev* d_sims = nullptr;
     uint32_t* d_base = nullptr;
@@ -68,6 +69,11 @@ struct BatchImpl {
     cudaGraphExec_t exec_pre = nullptr, exec_body = nullptr, exec_post = nullptr;
     uint32_t* d_flag = nullptr;
     uint32_t* h_flag = nullptr;
+    // persistent precision solve (one cooperative launch per substep)
+    GridBar* d_bar = nullptr;
+    bool persist_ok = true;
+    int persist_grid = 0;
+    uint32_t persist_guard = 0;
     double timeout_s = 600.0;
     std::string err;
     bool owned_by_sim = false;
@@ -81,6 +87,8 @@ struct BatchImpl {
     int capture();
     int record_pre(cudaStream_t st);
     int record_post(cudaStream_t st);
+    int record_gs_part(cudaStream_t st);     // scan .. divergence and the red-black sweeps
+    int record_post_solve(cudaStream_t st);  // project, g2p
     int step(uint32_t n);
     int wait();
     void drop_graphs();
@@ -199,12 +207,12 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
             L.nlev = mg_levels(n, L.dims);
             for (int l = 1; l < L.nlev; l++) {
                 const uint64_t c = uint64_t(L.dims[l][0]) * L.dims[l][1] * L.dims[l][2];
-                const uint64_t ch = (c + kScanChunk - 1) / kScanChunk;
+                const uint64_t ch = (c + kCoarseChunk - 1) / kCoarseChunk;
                 L.ltype[l] = take(c);
                 L.linfo[l] = take(2 * c);
                 L.lr[l] = take(4 * c);
                 L.lz[l] = take(4 * c);
-                L.llist[l] = take(4 * ch * kScanChunk);
+                L.llist[l] = take(4 * ch * kCoarseChunk);
                 L.llcnt[l] = take(8 * ch);
             }
         }
@@ -219,6 +227,7 @@ BatchImpl::~BatchImpl() {
     if (d_base) cudaFree(d_base);
     if (d_flag) cudaFree(d_flag);
     if (h_flag) cudaFreeHost(h_flag);
+    if (d_bar) cudaFree(d_bar);
     if (side) cudaStreamDestroy(side);
     if (side2) cudaStreamDestroy(side2);
     if (stream) cudaStreamDestroy(stream);
@@ -283,9 +292,9 @@ int BatchImpl::rebuild() {
         for (int l = 0; l < kMaxLevels; l++) {
             // global-memory smoothing of level l and restriction to l + 1 exist below the tail
             const bool has = mg && l < d.tail;
-            items[6 + l] = has ? cdiv(d.lev[l].nc, kScanChunk) : 0;
-            items[6 + kMaxLevels + l] = has ? cdiv(d.lev[l + 1].nc, kScanChunk) : 0;
-            items[6 + 2 * kMaxLevels + l] = (mg && l + 1 < d.nlev) ? cdiv(d.lev[l + 1].nc, kScanChunk) : 0;
+            items[6 + l] = has ? cdiv(d.lev[l].nc, d.lev[l].cs) : 0;
+            items[6 + kMaxLevels + l] = has ? cdiv(d.lev[l + 1].nc, d.lev[l + 1].cs) : 0;
+            items[6 + 2 * kMaxLevels + l] = (mg && l + 1 < d.nlev) ? cdiv(d.lev[l + 1].nc, d.lev[l + 1].cs) : 0;
         }
         for (int k = 0; k < kStages; k++) base[k * (n + 1) + i + 1] = base[k * (n + 1) + i] + items[k];
         if (d.solver == 0) {
@@ -304,6 +313,7 @@ int BatchImpl::rebuild() {
             else pw.any_jacobi = true;
         }
         timeout_s = std::max(timeout_s, s->opts.wait_timeout_s);
+        if (d.solver == 1) persist_guard = std::max(persist_guard, d.max_iter + 2);
     }
     if (timeout_s <= 0) timeout_s = 600.0;
     if ((e = cudaMemcpyAsync(d_sims, host.data(), n * sizeof(SimDev), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
@@ -328,9 +338,36 @@ int BatchImpl::rebuild() {
     pw.n_sims = n;
     pw.chunks = w_chunks;
     if (pw.any_mg && (e = mg_tail_attr(pw.tail_smem)) != cudaSuccess) return cuda_fail(e, "tail kernel attribute");
+    if (any_pcg && !d_bar) {
+        if ((e = cudaMalloc(&d_bar, sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
+        if ((e = cudaMemset(d_bar, 0, sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
+    }
+    if (any_pcg) persist_grid = pcg_solve_grid(pw.tail_smem);
     int rc = capture();
     if (rc) return rc;
     dirty = false;
+    return PXF_OK;
+}
+
+int BatchImpl::record_gs_part(cudaStream_t st) {
+    const int n = int(sims.size());
+    cudaError_t e;
+    if ((e = launch_scan(w_chunks, d_sims, n, st)) != cudaSuccess) return cuda_fail(e, "scan");
+    if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
+    if ((e = launch_p2g(w_tiles, tile_shape, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+    if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
+    if (any_gs) {
+        for (uint32_t it = 0; it < max_gs_iters; it++)
+            for (uint32_t parity = 0; parity < 2; parity++)
+                if ((e = launch_pressure_rb(w_half, parity, it, st)) != cudaSuccess) return cuda_fail(e, "pressure");
+    }
+    return PXF_OK;
+}
+
+int BatchImpl::record_post_solve(cudaStream_t st) {
+    cudaError_t e;
+    if ((e = launch_project(w_faces, st)) != cudaSuccess) return cuda_fail(e, "project");
+    if ((e = launch_g2p(w_parts, st)) != cudaSuccess) return cuda_fail(e, "g2p");
     return PXF_OK;
 }
 
@@ -409,6 +446,28 @@ static cudaError_t end_capture_to_exec(cudaStream_t st, cudaGraphExec_t* exec) {
 int BatchImpl::capture() {
     const int n = int(sims.size());
     cudaError_t e;
+    // PXF_PCG_PERSISTENT=0 selects the graph-of-kernels precision loop instead of the persistent
+    // cooperative solve.
+    static const bool no_persist = [] { const char* v = std::getenv("PXF_PCG_PERSISTENT"); return v && v[0] == '0'; }();
+    if (any_pcg && persist_ok && !no_persist && persist_grid > 0) {
+        if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return cuda_fail(e, "begin capture");
+        int rc = record_gs_part(stream);
+        cudaError_t el = rc ? cudaSuccess : launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream);
+        if (!rc && el == cudaSuccess) rc = record_post_solve(stream);
+        cudaGraphExec_t ex = nullptr;
+        e = end_capture_to_exec(stream, &ex);
+        if (!rc && el == cudaSuccess && e == cudaSuccess) {
+            exec = ex;
+            persistent = true;
+            return PXF_OK;
+        }
+        if (ex) cudaGraphExecDestroy(ex);
+        cudaGetLastError();
+        if (rc) return rc;
+        persist_ok = false;   // fall back to the graph-of-kernels loop
+    }
+    persistent = false;
     // PXF_NO_COND_GRAPH=1 selects the host-driven precision loop (its graphs have no conditional
     // node, which is what kernel profilers need to attribute the loop's kernels).
     static const bool no_cond = [] { const char* v = std::getenv("PXF_NO_COND_GRAPH"); return v && v[0] == '1'; }();
@@ -517,6 +576,12 @@ int BatchImpl::wait() {
         if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(spins > 4096 ? 500 : 20));
     }
     cudaEventDestroy(ev);
+    if (persistent && d_bar) {
+        GridBar hb;
+        e = cudaMemcpy(&hb, d_bar, sizeof(hb), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "grid barrier state");
+        if (hb.err) return fail(PXF_ETIMEDOUT, "the persistent pressure solve stopped: a grid barrier wait timed out");
+    }
     return PXF_OK;
 }
 
@@ -590,7 +655,11 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
                 size_t t = ev(); add("pressure_rb", prev, t); prev = t;
             }
     }
-    if (any_pcg) {
+    if (any_pcg && persistent) {
+        if ((e = launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream)) != cudaSuccess)
+            return cuda_fail(e, "pcg solve");
+        size_t t = ev(); add("pcg_solve_persistent", prev, t); prev = t;
+    } else if (any_pcg) {
         if (!d_flag) {
             if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
             if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
@@ -794,6 +863,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
         d.lev[0].info = d.info;
         d.lev[0].r = d.r;
         d.lev[0].z = d.z;
+        d.lev[0].cs = kScanChunk;
         d.lev[0].list = reinterpret_cast<uint32_t*>(m + L.llist[0]);
         d.lev[0].lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[0]);
         for (int l = 1; l < L.nlev; l++) {
@@ -804,6 +874,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
             v.info = reinterpret_cast<uint16_t*>(m + L.linfo[l]);
             v.r = reinterpret_cast<float*>(m + L.lr[l]);
             v.z = reinterpret_cast<float*>(m + L.lz[l]);
+            v.cs = kCoarseChunk;
             v.list = reinterpret_cast<uint32_t*>(m + L.llist[l]);
             v.lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[l]);
         }

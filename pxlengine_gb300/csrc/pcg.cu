@@ -13,19 +13,26 @@
 //     declared on that FP64 residual, |r| <= rtol |b|.
 // (GB300's FP64 pipe runs at about 1 TFLOP/s, 1/60 of FP32, so FP64 is kept out of per-cell work.)
 //
-// Reductions never use atomics or fences: every 2048-cell chunk writes its partial sums, and a
-// one-block control kernel per simulation sums them in chunk order and advances that simulation's
-// solver state. Results therefore do not depend on scheduling or on the other simulations of a
-// batch.
+// Work: every kernel iterates compacted, colour-split lists of the system cells of each chunk
+// (built once per substep with a block scan, so the order of every reduction is fixed). Partial
+// sums are per level-0 chunk; a control step per simulation sums them in chunk order and advances
+// that simulation's state. No atomics, no fences in the arithmetic: results do not depend on
+// scheduling or on the other simulations of a batch.
 //
 // Multigrid (level l+1 halves each axis, rounding up): a coarse cell is AIR if any child is AIR,
 // else FLUID if any child is FLUID, else SOLID (children outside the fine grid are SOLID); each
 // level's operator is the 7-point system above built from its own types. V-cycle: red-black
 // Gauss-Seidel pre-smoothing (red from zero, black), restriction r_c = 1/2 * sum of the children's
 // residuals, recursion, prolongation (each child += its parent's correction, fused into the first
-// post-smoothing sweep), post-smoothing (black, red). The coarsest level (<= 512 cells) runs
-// `coarse_iters` red-black then as many black-red iterations from zero in one block. Restriction
-// is prolongation^T / 2 and the sweeps mirror each other, so the cycle is symmetric.
+// post-smoothing sweep), post-smoothing (black, red). Levels with at most kTailCells cells run
+// inside one block in shared memory; the coarsest level (<= 512 cells) runs `coarse_iters`
+// red-black then as many black-red iterations from zero. Restriction is prolongation^T / 2 and the
+// sweeps mirror each other, so the cycle is symmetric.
+//
+// Execution: each step is a device "phase" function. The phases run either as separate kernels
+// (graph-captured, the loop as a conditional while-node) or all inside one persistent cooperative
+// kernel per substep with grid barriers between phases. Barrier waits are bounded: a wait that
+// exceeds its limit raises an error flag that the host reports, and every block returns.
 #include "pxf_device.cuh"
 #include "pxf_kernels.h"
 
@@ -34,7 +41,6 @@ namespace pxf {
 namespace {
 
 constexpr int THREADS = 256;
-constexpr int PER_THREAD = kScanChunk / THREADS;   // 8 cells per thread, strided by 256
 
 // ---------------------------------------------------------------- double-float arithmetic
 struct DF {
@@ -67,7 +73,7 @@ __device__ __forceinline__ double block_sum(DF a, double* sh) {
     __syncthreads();
     double out = 0;
     if (threadIdx.x == 0)
-        for (int k = 0; k < THREADS / 32; k++) out += sh[k];
+        for (int k = 0; k < int(blockDim.x >> 5); k++) out += sh[k];
     __syncthreads();
     return out;
 }
@@ -90,7 +96,7 @@ __device__ __forceinline__ float rhs_of(const SimDev& s, uint32_t c) {
     return s.div[c] * s.h * s.h / s.dt;   // fluid.slang:181
 }
 
-// Per-simulation scalars, written by the previous launch's control kernel: read through L2.
+// Per-simulation scalars, written by the previous step's control: read through L2.
 __device__ __forceinline__ uint32_t ldu(const uint32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldd(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ float ldf(const float* p) { return __ldcg(p); }
@@ -99,11 +105,11 @@ __device__ __forceinline__ bool active(const SimDev& s) { return s.solver == 1 &
 
 __device__ __forceinline__ uint32_t nchunks0(const SimDev& s) { return (s.nc + kScanChunk - 1) / kScanChunk; }
 
-// Fixed-order sum of a simulation's chunk partials (control kernels, one block per simulation).
+// Fixed-order sum of a simulation's chunk partials (one block per simulation).
 __device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
     const uint32_t n = nchunks0(s);
     double p = 0;
-    for (uint32_t k = threadIdx.x; k < n; k += THREADS) p += __ldcg(s.partial + k);
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) p += __ldcg(s.partial + k);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) p += __shfl_down_sync(0xffffffffu, p, d);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -111,7 +117,7 @@ __device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
     __syncthreads();
     double out = 0;
     if (threadIdx.x == 0)
-        for (int k = 0; k < THREADS / 32; k++) out += sh[k];
+        for (int k = 0; k < int(blockDim.x >> 5); k++) out += sh[k];
     __syncthreads();
     return out;
 }
@@ -119,18 +125,24 @@ __device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
 // Entries [lo, hi) of chunk `chunk` of a level's system-cell list for colour 0 (red), 1 (black)
 // or 2 (both).
 __device__ __forceinline__ void seg(const MgLevel& L, uint32_t chunk, int color, uint32_t& lo, uint32_t& hi) {
-    const uint32_t nr = __ldg(L.lcnt + 2 * chunk), nb = __ldg(L.lcnt + 2 * chunk + 1);
+    const uint32_t nr = __ldcg(L.lcnt + 2 * chunk), nb = __ldcg(L.lcnt + 2 * chunk + 1);
     lo = color == 1 ? nr : 0u;
     hi = color == 0 ? nr : nr + nb;
 }
 
+__device__ __forceinline__ const uint32_t* list_of(const MgLevel& L, uint32_t chunk) {
+    return L.list + size_t(chunk) * L.cs;
+}
+
 }  // namespace
 
-// ============================================================================ system-cell lists
-// Compacts each 2048-cell chunk of level l into its red then black system cells, in ascending
-// cell order (a block scan, so the order and every reduction over it are deterministic).
-__global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) {
-    __shared__ uint32_t wr[THREADS / 32], wb[THREADS / 32];
+// ============================================================================ phases
+// Every phase walks its work index with a block-strided loop, so it serves both the standalone
+// kernels and the persistent kernel.
+
+// Compacts each chunk of level l into its red then black system cells, in ascending cell order.
+__device__ void ph_cell_lists(const Work& w, int l) {
+    __shared__ uint32_t wr[32], wb[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
@@ -138,18 +150,17 @@ __global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) {
         const MgLevel L = sp->lev[l];
         const uint32_t chunk = item - w.base[si];
         const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
-        const uint32_t c0 = chunk * kScanChunk + threadIdx.x * PER_THREAD;
+        const uint32_t per = L.cs / blockDim.x;   // 8 on level 0, 1 below
+        const uint32_t c0 = chunk * L.cs + threadIdx.x * per;
         uint32_t redm = 0, blkm = 0;
-#pragma unroll
-        for (int k = 0; k < PER_THREAD; k++) {
+        for (uint32_t k = 0; k < per; k++) {
             const uint32_t c = c0 + k;
             if (c >= L.nc || !in_system(L.info[c])) continue;
             const uint32_t par = (c % nx + (c / nx) % ny + c / nxy) & 1u;
             if (par) blkm |= 1u << k; else redm |= 1u << k;
         }
         const uint32_t nr = __popc(redm), nb = __popc(blkm);
-        // block exclusive scans of nr and nb
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = int(blockDim.x >> 5);
         uint32_t xr = nr, xb = nb;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -159,15 +170,14 @@ __global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) {
         if (lane == 31) { wr[wid] = xr; wb[wid] = xb; }
         __syncthreads();
         uint32_t br = 0, bb = 0, tr = 0, tb = 0;
-        for (int k = 0; k < THREADS / 32; k++) {
+        for (int k = 0; k < nw; k++) {
             if (k < wid) { br += wr[k]; bb += wb[k]; }
             tr += wr[k];
             tb += wb[k];
         }
         uint32_t pr = br + xr - nr, pb = tr + bb + xb - nb;
-        uint32_t* out = L.list + size_t(chunk) * kScanChunk;
-#pragma unroll
-        for (int k = 0; k < PER_THREAD; k++) {
+        uint32_t* out = L.list + size_t(chunk) * L.cs;
+        for (uint32_t k = 0; k < per; k++) {
             if (redm & (1u << k)) out[pr++] = c0 + k;
             if (blkm & (1u << k)) out[pb++] = c0 + k;
         }
@@ -179,16 +189,16 @@ __global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) {
     }
 }
 
-// ============================================================================ multigrid setup
-// Type of level l+1 from its children on level l.
-__global__ void __launch_bounds__(THREADS) k_mg_coarsen(Work w, int l) {
+// Type of level l+1 from its children on level l (work: level-(l+1) chunks).
+__device__ void ph_coarsen(const Work& w, int l) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1) continue;
         const MgLevel F = sp->lev[l], Cc = sp->lev[l + 1];
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t P = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+        const uint32_t per = Cc.cs / blockDim.x;
+        for (uint32_t k = 0; k < per; k++) {
+            const uint32_t P = (item - w.base[si]) * Cc.cs + k * blockDim.x + threadIdx.x;
             if (P >= Cc.nc) continue;
             const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
             const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
@@ -207,14 +217,15 @@ __global__ void __launch_bounds__(THREADS) k_mg_coarsen(Work w, int l) {
 }
 
 // Neighbour record of level l+1 (as k_divergence builds it for level 0).
-__global__ void __launch_bounds__(THREADS) k_mg_info(Work w, int l) {
+__device__ void ph_info(const Work& w, int l) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1) continue;
         const MgLevel L = sp->lev[l + 1];
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+        const uint32_t per = L.cs / blockDim.x;
+        for (uint32_t k = 0; k < per; k++) {
+            const uint32_t c = (item - w.base[si]) * L.cs + k * blockDim.x + threadIdx.x;
             if (c >= L.nc) continue;
             uint16_t info = 0;
             if (L.type[c] == FLUID) {
@@ -239,13 +250,12 @@ __global__ void __launch_bounds__(THREADS) k_mg_info(Work w, int l) {
     }
 }
 
-// ============================================================================ V-cycle
-// One red-black half sweep of A z = r on level l over the cells of one colour.
+// One red-black half sweep of A z = r on level l over the system cells of one colour.
 // mode 0: z = (r + sum z_n) / cnt; mode 1: the other colour is zero (z = r / cnt);
 // mode 2: as 0 with the coarse correction of level l+1 added to every neighbour on the fly
 // (fused prolongation); mode 3: as 0, then the chunk's partial r.z over all system cells.
-__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode) {
-    __shared__ double sh[8];
+__device__ void ph_smooth(const Work& w, int l, int color, int mode) {
+    __shared__ double sh[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
@@ -257,11 +267,14 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
         const uint32_t cnx = uint32_t(Cc.nx), cnxy = uint32_t(Cc.nx) * uint32_t(Cc.ny);
         uint32_t lo, hi;
         seg(L, chunk, color, lo, hi);
-        const uint32_t* lst = L.list + size_t(chunk) * kScanChunk;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+        const uint32_t* __restrict__ lst = list_of(L, chunk);
+        const uint16_t* __restrict__ info = L.info;
+        const float* __restrict__ r = L.r;
+        float* __restrict__ z = L.z;
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
-            const uint32_t inf = L.info[c];
-            float sum = L.r[c];
+            const uint32_t inf = info[c];
+            float sum = r[c];
             if (mode == 2) {
                 const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
 #pragma unroll
@@ -271,7 +284,7 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
                     const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
                     const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
                     const uint32_t n = uint32_t(int64_t(c) + dx + int64_t(dy) * nx + int64_t(dz) * nxy);
-                    float zn = L.z[n];
+                    float zn = z[n];
                     const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
                                        cnxy * (uint32_t(int(kk) + dz) >> 1);
                     if (in_system(Cc.info[P])) zn += Cc.z[P];
@@ -280,9 +293,9 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
             } else if (mode != 1) {
 #pragma unroll
                 for (int q = 0; q < 6; q++)
-                    if (inf & (1u << q)) sum += L.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+                    if (inf & (1u << q)) sum += z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
             }
-            L.z[c] = sum / cnt_of(inf);
+            z[c] = sum / cnt_of(inf);
         }
         if (mode == 3) {
             // r.z over every system cell of the chunk (the other colour was final before this sweep).
@@ -290,9 +303,9 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
             DF acc{0.f, 0.f};
             uint32_t a0, a1;
             seg(L, chunk, 2, a0, a1);
-            for (uint32_t e = a0 + threadIdx.x; e < a1; e += THREADS) {
+            for (uint32_t e = a0 + threadIdx.x; e < a1; e += blockDim.x) {
                 const uint32_t c = lst[e];
-                acc = df_add(acc, two_prod(L.r[c], L.z[c]));
+                acc = df_add(acc, two_prod(r[c], z[c]));
             }
             const double t = block_sum(acc, sh);
             if (threadIdx.x == 0) sp->partial[chunk] = t;
@@ -300,8 +313,9 @@ __global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color,
     }
 }
 
-// r_{l+1} = 1/2 * sum over the children of their residual r - A z (level l).
-__global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
+// r_{l+1} = 1/2 * sum over the children of their residual r - A z (level l); 8 lanes per coarse
+// cell, children summed by a fixed shuffle tree. Work: level-(l+1) chunks.
+__device__ void ph_restrict(const Work& w, int l) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
@@ -311,10 +325,10 @@ __global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
         const uint32_t chunk = item - w.base[si];
         uint32_t lo, hi;
         seg(Cc, chunk, 2, lo, hi);
-        const uint32_t* lst = Cc.list + size_t(chunk) * kScanChunk;
-        // 8 consecutive lanes per coarse cell, one child each.
+        const uint32_t* lst = list_of(Cc, chunk);
         const uint32_t chd = threadIdx.x & 7u;
-        for (uint32_t base = lo; base < hi; base += THREADS / 8) {
+        const uint32_t per_pass = blockDim.x / 8;
+        for (uint32_t base = lo; base < hi; base += per_pass) {
             const uint32_t e = base + (threadIdx.x >> 3);
             float res = 0.0f;
             uint32_t P = 0;
@@ -346,9 +360,8 @@ __global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) {
 
 // ------------------------------------------------------------------ shared-memory tail
 // Levels tail..nlev-1 (the tail level holds at most kTailCells cells) run as one V-cycle inside
-// one block, in shared memory: same sweeps, restriction, fused prolongation and coarsest solve as
-// the global-memory path. Input r of the tail level, output z of the tail level; when the tail is
-// level 0 the block also writes the level-0 chunk partials of r.z.
+// one block per simulation, in shared memory. Input r of the tail level, output z of the tail
+// level; when the tail is level 0 the block also writes the level-0 chunk partials of r.z.
 struct TailLevel {
     int nx, ny, nz;
     uint32_t nc;
@@ -359,13 +372,13 @@ struct TailLevel {
 
 __device__ void tail_smooth(const TailLevel& L, const MgLevel& G, uint32_t color, int mode, const TailLevel* C) {
     const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
-    const uint32_t nch = (L.nc + kScanChunk - 1) / kScanChunk;
+    const uint32_t nch = (L.nc + G.cs - 1) / G.cs;
     for (uint32_t ch = 0; ch < nch; ch++) {
         uint32_t lo, hi;
         seg(G, ch, int(color), lo, hi);
-        const uint32_t* lst = G.list + size_t(ch) * kScanChunk;
+        const uint32_t* lst = list_of(G, ch);
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const uint32_t c = __ldg(lst + e);
+            const uint32_t c = __ldcg(lst + e);
             const uint32_t inf = L.info[c];
             float sum = L.r[c];
             if (mode == 2) {
@@ -396,13 +409,13 @@ __device__ void tail_smooth(const TailLevel& L, const MgLevel& G, uint32_t color
 
 __device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc, const MgLevel& GC) {
     const uint32_t nx = uint32_t(F.nx), nxy = uint32_t(F.nx) * uint32_t(F.ny);
-    const uint32_t nch = (Cc.nc + kScanChunk - 1) / kScanChunk;
+    const uint32_t nch = (Cc.nc + GC.cs - 1) / GC.cs;
     for (uint32_t ch = 0; ch < nch; ch++) {
         uint32_t lo, hi;
         seg(GC, ch, 2, lo, hi);
-        const uint32_t* lst = GC.list + size_t(ch) * kScanChunk;
+        const uint32_t* lst = list_of(GC, ch);
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const uint32_t P = __ldg(lst + e);
+            const uint32_t P = __ldcg(lst + e);
             const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
             const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
             float sum = 0.0f;
@@ -425,8 +438,7 @@ __device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc, const MgL
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims) {
-    extern __shared__ float tsm[];
+__device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
     __shared__ double sh[32];
     for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
         const SimDev* sp = sims + si;
@@ -442,11 +454,11 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims
             lv[l].z = base + g.nc;
             lv[l].info = reinterpret_cast<uint16_t*>(base + 2 * g.nc);
             base += 2 * g.nc + (g.nc + 1) / 2;
-            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[l].info[c] = g.info[c];
+            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[l].info[c] = __ldcg(g.info + c);
         }
         {
             const MgLevel g = sp->lev[T];
-            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[T].r[c] = g.r[c];
+            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[T].r[c] = __ldcg(g.r + c);
         }
         __syncthreads();
         for (int l = T; l + 1 < NL; l++) {
@@ -473,24 +485,14 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims
         }
         if (T == 0) {
             // level-0 chunk partials of r.z (the tail holds the whole level)
-            const uint32_t nch = (sp->nc + kScanChunk - 1) / kScanChunk;
+            const uint32_t nch = nchunks0(*sp);
             for (uint32_t ch = 0; ch < nch; ch++) {
                 DF acc{0.f, 0.f};
-                for (uint32_t c = ch * kScanChunk + threadIdx.x; c < min((ch + 1) * kScanChunk, sp->nc); c += blockDim.x)
+                const uint32_t end = min((ch + 1) * kScanChunk, sp->nc);
+                for (uint32_t c = ch * kScanChunk + threadIdx.x; c < end; c += blockDim.x)
                     if (in_system(lv[0].info[c])) acc = df_add(acc, two_prod(lv[0].r[c], lv[0].z[c]));
-#pragma unroll
-                for (int d = 16; d > 0; d >>= 1) {
-                    const DF t{__shfl_down_sync(0xffffffffu, acc.hi, d), __shfl_down_sync(0xffffffffu, acc.lo, d)};
-                    acc = df_add(acc, t);
-                }
-                if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = double(acc.hi) + double(acc.lo);
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    double t = 0;
-                    for (int k = 0; k < int(blockDim.x >> 5); k++) t += sh[k];
-                    sp->partial[ch] = t;
-                }
-                __syncthreads();
+                const double t = block_sum(acc, sh);
+                if (threadIdx.x == 0) sp->partial[ch] = t;
             }
         }
         __syncthreads();
@@ -498,8 +500,8 @@ __global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims
 }
 
 // Jacobi preconditioner: z = r / cnt, partial r.z.
-__global__ void __launch_bounds__(THREADS) k_jacobi(Work w) {
-    __shared__ double sh[8];
+__device__ void ph_jacobi(const Work& w) {
+    __shared__ double sh[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -508,8 +510,8 @@ __global__ void __launch_bounds__(THREADS) k_jacobi(Work w) {
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+        const uint32_t* lst = list_of(s.lev[0], chunk);
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
             const float r = s.r[c];
@@ -522,10 +524,9 @@ __global__ void __launch_bounds__(THREADS) k_jacobi(Work w) {
     }
 }
 
-// ============================================================================ CG kernels
 // Partial |b|^2.
-__global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) {
-    __shared__ double sh[8];
+__device__ void ph_init(const Work& w) {
+    __shared__ double sh[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -534,10 +535,9 @@ __global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) {
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
-            const uint32_t c = lst[e];
-            const float b = rhs_of(s, c);
+        const uint32_t* lst = list_of(s.lev[0], chunk);
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+            const float b = rhs_of(s, lst[e]);
             acc = df_add(acc, two_prod(b, b));
         }
         const double t = block_sum(acc, sh);
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) {
 }
 
 // x64 = hi + lo for simulations about to restart (or x = 0 for a zero right-hand side).
-__global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) {
+__device__ void ph_widen(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -555,8 +555,8 @@ __global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) {
         const uint32_t chunk = item - w.base[si];
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+        const uint32_t* lst = list_of(s.lev[0], chunk);
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             if (zero) {
                 s.x2[c] = make_float2(0.f, 0.f);
@@ -570,8 +570,8 @@ __global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) {
 }
 
 // FP64 restart residual r = b - A x and its partial |r|^2.
-__global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) {
-    __shared__ double sh[8];
+__device__ void ph_resid(const Work& w) {
+    __shared__ double sh[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -581,8 +581,8 @@ __global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) {
         double rr = 0;
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* lst = s.lev[0].list + size_t(chunk) * kScanChunk;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+        const uint32_t* lst = list_of(s.lev[0], chunk);
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
             double ax = double(cnt_of(inf)) * s.x64[c];
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) {
         __syncthreads();
         if (threadIdx.x == 0) {
             double t = 0;
-            for (int k2 = 0; k2 < THREADS / 32; k2++) t += sh[k2];
+            for (int k2 = 0; k2 < int(blockDim.x >> 5); k2++) t += sh[k2];
             s.partial[chunk] = t;
         }
         __syncthreads();
@@ -608,8 +608,8 @@ __global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) {
 
 // p' = z + beta p (p' = z after a restart); Ap = A p' (neighbours' p' formed on the fly);
 // partial p'.Ap.
-__global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) {
-    __shared__ double sh[8];
+__device__ void ph_dir(const Work& w) {
+    __shared__ double sh[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -628,12 +628,11 @@ __global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) {
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* __restrict__ lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
 #pragma unroll 2
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             const uint32_t inf = info[c];
-            // p' = z (fresh) or z + beta p: with beta = 0 the fresh case reads pold but ignores it
             const float pn = fresh ? z[c] : z[c] + beta * pold[c];
             float ap = cnt_of(inf) * pn;
 #pragma unroll
@@ -653,8 +652,8 @@ __global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) {
 }
 
 // x += alpha p (double-float), r -= alpha Ap (FP32), partial |r|^2.
-__global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) {
-    __shared__ double sh[8];
+__device__ void ph_update(const Work& w) {
+    __shared__ double sh[32];
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
@@ -670,9 +669,9 @@ __global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) {
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        const uint32_t* __restrict__ lst = s.lev[0].list + size_t(chunk) * kScanChunk;
+        const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
 #pragma unroll 2
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += THREADS) {
+        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             const float pc = p[c];
             DF d = two_prod(ah, pc);
@@ -689,14 +688,14 @@ __global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) {
     }
 }
 
-// FP32 pressure copy and the FP64 solution at the end of the solve.
-__global__ void __launch_bounds__(THREADS) k_pcg_finish(Work w) {
+// FP32 pressure copy and the FP64 solution at the end of the solve (all cells).
+__device__ void ph_finish(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
-        for (int k = 0; k < PER_THREAD; k++) {
-            const uint32_t c = (item - w.base[si]) * kScanChunk + k * THREADS + threadIdx.x;
+        for (uint32_t k = 0; k < kScanChunk / blockDim.x; k++) {
+            const uint32_t c = (item - w.base[si]) * kScanChunk + k * blockDim.x + threadIdx.x;
             if (c >= s.nc) continue;
             double x = 0.0;
             if (in_system(s.info[c])) {
@@ -709,11 +708,11 @@ __global__ void __launch_bounds__(THREADS) k_pcg_finish(Work w) {
     }
 }
 
-// ============================================================================ control kernels
-// One block per simulation; each sums the partials of the step before it and advances the state.
-// phase 0: after |b|^2   1: after the restart residual   2: after r.z   3: after p.Ap   4: after |r|^2
-__global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_sims, int phase) {
-    __shared__ double sh[8];
+// Control: one block per simulation sums the partials of the step before it and advances the
+// state. phase 0: after |b|^2   1: after the restart residual   2: after r.z   3: after p.Ap
+// 4: after |r|^2
+__device__ void ph_ctl(const SimDev* sims, int n_sims, int phase) {
+    __shared__ double sh[32];
     for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
         const SimDev& s = sims[si];
         if (s.solver != 1) continue;
@@ -786,34 +785,167 @@ __global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_s
     }
 }
 
+__device__ __forceinline__ bool any_active(const SimDev* sims, int n_sims) {
+    for (int i = 0; i < n_sims; i++)
+        if (sims[i].solver == 1 && !__ldcg(&sims[i].pcg->done)) return true;
+    return false;
+}
+
+__device__ __forceinline__ bool any_restart(const SimDev* sims, int n_sims) {
+    for (int i = 0; i < n_sims; i++)
+        if (sims[i].solver == 1 && !__ldcg(&sims[i].pcg->done) && __ldcg(&sims[i].pcg->restart_now)) return true;
+    return false;
+}
+
+// ============================================================================ standalone kernels
+__global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) { ph_cell_lists(w, l); }
+__global__ void __launch_bounds__(THREADS) k_mg_coarsen(Work w, int l) { ph_coarsen(w, l); }
+__global__ void __launch_bounds__(THREADS) k_mg_info(Work w, int l) { ph_info(w, l); }
+__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode) { ph_smooth(w, l, color, mode); }
+__global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) { ph_restrict(w, l); }
+__global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims) {
+    extern __shared__ float tsm[];
+    ph_tail(sims, n_sims, tsm);
+}
+__global__ void __launch_bounds__(THREADS) k_jacobi(Work w) { ph_jacobi(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) { ph_init(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) { ph_widen(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) { ph_resid(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) { ph_dir(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) { ph_update(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_finish(Work w) { ph_finish(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_sims, int phase) { ph_ctl(sims, n_sims, phase); }
+
 __global__ void k_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    unsigned any = 0;
-    for (int i = 0; i < n_sims; i++) {
-        const SimDev& s = sims[i];
-        if (s.solver == 1 && !__ldcg(&s.pcg->done)) any = 1;
-    }
-    cudaGraphSetConditional(h, any);
+    cudaGraphSetConditional(h, any_active(sims, n_sims) ? 1u : 0u);
 }
 
 __global__ void k_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    unsigned any = 0;
-    for (int i = 0; i < n_sims; i++) {
-        const SimDev& s = sims[i];
-        if (s.solver == 1 && !__ldcg(&s.pcg->done) && __ldcg(&s.pcg->restart_now)) any = 1;
-    }
-    cudaGraphSetConditional(h, any);
+    cudaGraphSetConditional(h, any_restart(sims, n_sims) ? 1u : 0u);
 }
 
 __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    uint32_t any = 0;
-    for (int i = 0; i < n_sims; i++) {
-        const SimDev& s = sims[i];
-        if (s.solver == 1 && !__ldcg(&s.pcg->done)) any = 1;
+    *flag = any_active(sims, n_sims) ? 1u : 0u;
+}
+
+// ============================================================================ persistent solve
+// Grid barrier with a bounded wait: arrive on a counter, the last block advances the generation;
+// the others poll it with a cycle limit. A timed-out wait sets `err`; every block then leaves.
+__device__ __forceinline__ bool grid_sync(GridBar* b) {
+    __shared__ int bad;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned g = __ldcg(&b->gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(&b->count, 1u);
+        if (arrived == gridDim.x - 1) {
+            b->count = 0;
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (__ldcg(&b->gen) == g) {
+                if (__ldcg(&b->err) || clock64() - t0 > kBarrierCycles) {
+                    atomicExch(&b->err, 1u);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        bad = __ldcg(&b->err) != 0;
     }
-    *flag = any;
+    __syncthreads();
+    return !bad;
+}
+
+struct SolveArgs {
+    PcgWork pw;
+    GridBar* bar;
+    uint32_t guard;   // bound on the CG loop (largest iteration cap of the batch + 2)
+};
+
+#define SYNC_OR_RETURN() \
+    if (!grid_sync(a.bar)) return
+
+__device__ bool solve_precond(const SolveArgs& a, float* tsm) {
+    const PcgWork& pw = a.pw;
+    if (pw.any_jacobi) {
+        ph_jacobi(pw.chunks);
+        if (!grid_sync(a.bar)) return false;
+    }
+    if (pw.any_mg) {
+        for (int l = 0; l + 1 < pw.max_levels; l++) {
+            if (!pw.level[l].total) continue;
+            ph_smooth(pw.level[l], l, 0, 1);
+            if (!grid_sync(a.bar)) return false;
+            ph_smooth(pw.level[l], l, 1, 0);
+            if (!grid_sync(a.bar)) return false;
+            ph_restrict(pw.coarse[l], l);
+            if (!grid_sync(a.bar)) return false;
+        }
+        ph_tail(pw.sims, pw.n_sims, tsm);
+        if (!grid_sync(a.bar)) return false;
+        for (int l = pw.max_levels - 2; l >= 0; l--) {
+            if (!pw.level[l].total) continue;
+            ph_smooth(pw.level[l], l, 1, 2);
+            if (!grid_sync(a.bar)) return false;
+            ph_smooth(pw.level[l], l, 0, l == 0 ? 3 : 0);
+            if (!grid_sync(a.bar)) return false;
+        }
+    }
+    ph_ctl(pw.sims, pw.n_sims, 2);
+    return grid_sync(a.bar);
+}
+
+__device__ bool solve_restart(const SolveArgs& a) {
+    const PcgWork& pw = a.pw;
+    ph_widen(pw.chunks);
+    if (!grid_sync(a.bar)) return false;
+    ph_resid(pw.chunks);
+    if (!grid_sync(a.bar)) return false;
+    ph_ctl(pw.sims, pw.n_sims, 1);
+    return grid_sync(a.bar);
+}
+
+__global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
+    extern __shared__ float tsm[];
+    const PcgWork& pw = a.pw;
+    // multigrid setup: system-cell lists and the coarse levels
+    ph_cell_lists(pw.chunks, 0);
+    SYNC_OR_RETURN();
+    for (int l = 0; l + 1 < pw.setup_levels; l++) {
+        if (!pw.setup[l].total) continue;
+        ph_coarsen(pw.setup[l], l);
+        SYNC_OR_RETURN();
+        ph_info(pw.setup[l], l);
+        SYNC_OR_RETURN();
+        ph_cell_lists(pw.setup[l], l + 1);
+        SYNC_OR_RETURN();
+    }
+    ph_init(pw.chunks);
+    SYNC_OR_RETURN();
+    ph_ctl(pw.sims, pw.n_sims, 0);
+    SYNC_OR_RETURN();
+    if (!solve_restart(a)) return;
+    if (!solve_precond(a, tsm)) return;
+    for (uint32_t guard = 0; guard < a.guard; guard++) {
+        if (!any_active(pw.sims, pw.n_sims)) break;
+        ph_dir(pw.chunks);
+        SYNC_OR_RETURN();
+        ph_ctl(pw.sims, pw.n_sims, 3);
+        SYNC_OR_RETURN();
+        ph_update(pw.chunks);
+        SYNC_OR_RETURN();
+        ph_ctl(pw.sims, pw.n_sims, 4);
+        SYNC_OR_RETURN();
+        if (any_restart(pw.sims, pw.n_sims) && !solve_restart(a)) return;
+        if (!solve_precond(a, tsm)) return;
+    }
+    ph_finish(pw.chunks);
 }
 
 // ============================================================================ launchers
@@ -837,7 +969,9 @@ static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st) {
 }
 
 cudaError_t mg_tail_attr(size_t smem) {
-    return cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = cudaFuncSetAttribute(k_mg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pcg_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    return e;
 }
 
 cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
@@ -919,6 +1053,34 @@ cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaS
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st) {
     k_pcg_finish<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
     return cudaGetLastError();
+}
+
+// Blocks of the persistent solve that are guaranteed co-resident on this device.
+int pcg_solve_grid(size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_solve, THREADS, smem) != cudaSuccess) return 0;
+    if (per_sm > 4) per_sm = 4;
+    return per_sm * sm_count();
+}
+
+cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(&bar->err, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    SolveArgs a;
+    a.pw = pw;
+    a.bar = bar;
+    a.guard = guard;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(grid));
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = pw.tail_smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_pcg_solve, a);
 }
 
 }  // namespace pxf

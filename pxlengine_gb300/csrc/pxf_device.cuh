@@ -47,8 +47,10 @@ struct MgLevel {
     uint16_t* info;
     float* r;
     float* z;
-    // System cells of each 2048-cell chunk, in ascending order: chunk k owns list[2048 k ...],
-    // first its red cells ((i + j + k) even), then its black cells; lcnt[2k], lcnt[2k+1] count them.
+    // System cells of each chunk of `cs` cells (2048 on level 0, 256 below), in ascending order:
+    // chunk k owns list[cs k ...], first its red cells ((i + j + k) even), then its black cells;
+    // lcnt[2k], lcnt[2k+1] count them.
+    uint32_t cs;
     uint32_t* list;
     uint32_t* lcnt;
 };
@@ -87,10 +89,10 @@ struct SimDev {
 // Work index of one stage over a batch: item i of the stage belongs to simulation s where
 // base[s] <= i < base[s + 1].
 struct Work {
-    const SimDev* sims;
-    const uint32_t* base;
-    int n_sims;
-    uint32_t total;
+    const SimDev* sims = nullptr;
+    const uint32_t* base = nullptr;   // n_sims + 1 entries, device memory
+    int n_sims = 0;
+    uint32_t total = 0;
 };
 
 __device__ __forceinline__ int find_sim(const Work& w, uint32_t item) {

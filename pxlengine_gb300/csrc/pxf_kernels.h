@@ -3,17 +3,12 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pxf_device.cuh"
+
 namespace pxf {
 
-struct SimDev;
-
-// Device-resident work index of one stage (see Work in pxf_device.cuh).
-struct StageWork {
-    const SimDev* sims = nullptr;
-    const uint32_t* base = nullptr;   // n_sims + 1 entries, device memory
-    int n_sims = 0;
-    uint32_t total = 0;
-};
+// Device-resident work index of one stage.
+using StageWork = Work;
 
 constexpr uint32_t kScanChunk = 2048;     // cells per scan / precision-solver work item
 constexpr uint32_t kElemItem = 256;       // elements per item of the per-element kernels
@@ -51,8 +46,22 @@ struct PcgWork {
     size_t tail_smem = 0;               // dynamic shared memory of the tail kernel
 };
 
-constexpr uint32_t kTailCells = 8192;   // the shared-memory tail starts at the first level this small
+constexpr uint32_t kTailCells = 1024;   // the shared-memory tail starts at the first level this small
+constexpr uint32_t kCoarseChunk = 256;  // list chunk of the levels below level 0
 cudaError_t mg_tail_attr(size_t smem);
+
+// Grid barrier of the persistent solve (device memory, zero-initialised).
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+    unsigned err;      // set when a wait exceeded kBarrierCycles
+    unsigned pad;
+};
+constexpr long long kBarrierCycles = 4000000000LL;   // about 2 s at the GB300's clock
+
+// One cooperative launch that runs the whole precision solve of a substep.
+int pcg_solve_grid(size_t smem);
+cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st);
 
 // Precision solver: multigrid setup + |b|^2 + state reset + first restart + first z = M^-1 r;
 // then the loop body (direction + SpMV, update, conditional FP64 restart, preconditioner) while
