@@ -107,6 +107,11 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from
+# one ncu capture of this workload, keyed by (config, kernel); the capture is summarised in profiles/.
+KERNEL_TRAFFIC = {}
+
+
 def make_fluid(P, cfg):
     return P.Fluid("bench", [list(cfg["bounds"][0]), list(cfg["bounds"][1])],
                    [P.FluidBlock(list(a), list(b)) for a, b in cfg["fill"]], resolution=cfg["resolution"],
@@ -121,20 +126,27 @@ def workload_config(name, cfg, dims, n):
             "parallelism": "replicas"}
 
 
-def alg_bytes(stage, N, F, C, Cf):
-    """Algorithmic bytes of one launch of a stage (4 B per face / cell value, 32 B per particle)."""
+def kernel_bytes(kernel, N, F, C, Cf):
+    """Algorithmic bytes of one launch of a kernel: each array the kernel must touch counted once,
+    4 B per face or cell value, 32 B per particle, 1 B per cell flag (Cf = system cells)."""
     return {
-        "scan+classify": 4 * C + 8 * C + 1 * C,       # counts in, starts + flags out
-        "scatter": 64 * N,                           # particles in and out
-        "p2g": 32 * N + 8 * F,                       # sorted particles in, vel + vel_old out
-        "divergence": 4 * F + 1 * C + 4 * C + 2 * C,  # faces + flags in, divergence + neighbour record out
-        "pressure_rb": 8 * C,                        # half the cells: p of the other colour, div, p out (16C / iteration)
-        "pcg_dir_spmv": 2 * C + 16 * Cf,             # info sweep; r, p in; p', Ap out over system cells
-        "pcg_update": 2 * C + 32 * Cf,               # info sweep; x64 in/out, p, Ap, r in, r out
-        "pcg_restart": 2 * C + 16 * Cf,
-        "project": 8 * F + 8 * C,
-        "g2p": 64 * N + 8 * F,
-    }.get(stage)
+        "k_scan_apply": 4 * C + 4 * C + 1 * C,       # counts in; starts and cell flags out
+        "k_scatter": 64 * N,                         # particle records in and out (sorted order)
+        "k_p2g": 32 * N + 8 * F + 4 * C,             # sorted particles and cell starts in; vel, vel_old out
+        "k_divergence": 4 * F + 1 * C + 4 * C + 2 * C,   # faces, flags in; divergence, neighbour record out
+        "k_pressure_rb": 8 * C,                      # one colour: 16C per red-black iteration
+        "k_pcg_dir": 18 * Cf,                        # z, p, neighbour record in; p, Ap out
+        "k_pcg_update": 32 * Cf,                     # p, Ap, r, double-float x in; r, x out
+        "k_project": 8 * F + 5 * C,                  # faces in and out; pressure, flags in
+        "k_g2p": 64 * N + 8 * F,                     # particles in and out; vel, vel_old in
+    }.get(kernel)
+
+
+def substep_bytes(N, F, C, Cf, solver, iters):
+    """Algorithmic bytes of one substep: 96N + 60F + 40C plus the pressure solve (red-black GS:
+    16C per iteration; PCG: 56 B per system cell per iteration)."""
+    press = 16 * C * iters if solver == "gs" else 56 * Cf * iters
+    return 96 * N + 60 * F + 40 * C + press
 
 
 def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1):
@@ -232,31 +244,44 @@ def main():
         ms = float(t.item())
     value = N * args.steps * world / (ms / 1e3)
 
-    # Roofline of the dominant stage from a stage-by-stage substep (CUDA events on the library's stream).
+    # Roofline of the dominant kernel: a kernel-by-kernel substep with a CUDA event after every
+    # kernel on the library's stream (eager launches behind a hold kernel, so gaps are device time).
     roofline = None
-    stages = []
+    substep_roofline = None
+    kernels = []
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    iters = cfg["iterations"]
+    if cfg["solver"] == "pcg":
+        iters = sim.solver_stats()[0]
+    ct = sim.read_grid("cell_type")
+    Cf = int(np.count_nonzero(ct == 1))
     if not args.no_profile:
         prof = sim.profile_substep()
-        ct = sim.read_grid("cell_type")
-        Cf = int(np.count_nonzero(ct == 1))
-        stages = [{"stage": n, "launches": k, "ms": m} for n, k, m in prof]
-        top = max(prof, key=lambda r: r[2])
-        name, launches, tot = top
-        per_launch = alg_bytes(name, N, F, C, Cf)
-        peaks = {}
-        try:
-            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-                peaks = json.load(f)
-        except OSError:
-            pass
-        peak = peaks.get("hbm_gbs", 6800.0)
-        if per_launch:
+        total = sum(r[2] for r in prof)
+        kernels = [{"kernel": n, "launches": k, "ms": m, "share": m / total} for n, k, m in prof]
+        ranked = sorted(prof, key=lambda r: -r[2])
+        top = next((r for r in ranked if kernel_bytes(r[0], N, F, C, Cf)), None)
+        if top:
+            name, launches, tot = top
+            per_launch = kernel_bytes(name, N, F, C, Cf)
             achieved = per_launch / (tot / launches / 1e3) / 1e9
             roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": None,
-                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                        "alg_bytes_per_launch": per_launch, "launches_per_substep": launches,
-                        "avg_launch_us": 1e3 * tot / launches, "share_of_substep": tot / sum(r[2] for r in prof)}
+                        "frac": achieved / peak, "traffic": KERNEL_TRAFFIC.get((args.config, name)),
+                        "peak_source": peak_src, "alg_bytes_per_launch": per_launch,
+                        "launches_per_substep": launches, "avg_launch_us": 1e3 * tot / launches,
+                        "share_of_substep": tot / total, "largest_kernel": ranked[0][0]}
+    B = substep_bytes(N, F, C, Cf, cfg["solver"], iters)
+    achieved = B / (ms / args.steps / 1e3) / 1e9
+    substep_roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "alg_bytes_per_substep": B, "pressure_iterations": iters, "system_cells": Cf,
+                        "peak_source": peak_src}
 
     # End to end through the C ABI with pinned host buffers, one frame per step.
     e2e = None
@@ -282,7 +307,7 @@ def main():
         hb_in.close()
         hb_out.close()
 
-    launches_per_substep = sum(s["launches"] for s in stages) if stages else None
+    launches_per_substep = sum(k["launches"] for k in kernels) if kernels else None
     solver_stats = None
     if cfg["solver"] == "pcg":
         it, rel, st = sim.solver_stats()
@@ -299,9 +324,10 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam break, reference LCG seeding)",
                 "config": workload_config(args.config, cfg, sim.dims, N), "roofline": roofline,
+                "substep_roofline": substep_roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": (launches_per_substep * args.steps) if launches_per_substep else None,
-                "solver": solver_stats, "stages": stages, "wall_s_timed": t_wall}
+                "solver": solver_stats, "kernels": kernels, "wall_s_timed": t_wall}
         print(json.dumps(line), flush=True)
     sim.close()
     if dist:

@@ -307,7 +307,7 @@ int BatchImpl::rebuild() {
                 pw.max_levels = std::max(pw.max_levels, d.tail + 1);
                 pw.setup_levels = std::max(pw.setup_levels, d.nlev);
                 size_t bytes = 0;
-                for (int l = d.tail; l < d.nlev; l++) bytes += 4 * (2 * size_t(d.lev[l].nc) + (d.lev[l].nc + 1) / 2);
+                for (int l = d.tail; l < d.nlev; l++) bytes += 4 * size_t(tail_level_floats(d.lev[l].nc));
                 pw.tail_smem = std::max(pw.tail_smem, bytes);
             }
             else pw.any_jacobi = true;
@@ -446,10 +446,12 @@ static cudaError_t end_capture_to_exec(cudaStream_t st, cudaGraphExec_t* exec) {
 int BatchImpl::capture() {
     const int n = int(sims.size());
     cudaError_t e;
-    // PXF_PCG_PERSISTENT=0 selects the graph-of-kernels precision loop instead of the persistent
-    // cooperative solve.
-    static const bool no_persist = [] { const char* v = std::getenv("PXF_PCG_PERSISTENT"); return v && v[0] == '0'; }();
-    if (any_pcg && persist_ok && !no_persist && persist_grid > 0) {
+    // The precision loop is a graph of kernels (a conditional WHILE node around one CG iteration);
+    // PXF_PCG_PERSISTENT=1, read at each capture, selects the persistent cooperative solve instead
+    // (one launch, grid barriers between phases; slower on one large simulation).
+    const char* persist_env = std::getenv("PXF_PCG_PERSISTENT");
+    const bool want_persist = persist_env && persist_env[0] == '1';
+    if (any_pcg && persist_ok && want_persist && persist_grid > 0) {
         if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
             return cuda_fail(e, "begin capture");
         int rc = record_gs_part(stream);
@@ -610,94 +612,117 @@ int BatchImpl::step(uint32_t nsteps) {
     return PXF_OK;
 }
 
-// One substep launched stage by stage with events between the launches (eager, no graph).
+// Records an event after every kernel the library launches on the simulation's stream, so each
+// kernel's device time is the gap to the event before it.
+struct KernelTimer : LaunchLog {
+    cudaStream_t stream;
+    std::vector<cudaEvent_t> evs;
+    std::vector<std::pair<size_t, const char*>> spans;   // (index of the event ending the kernel, name)
+    size_t prev = 0;
+    bool ok = true;
+    explicit KernelTimer(cudaStream_t s) : stream(s) {}
+    ~KernelTimer() {
+        for (auto& e : evs) cudaEventDestroy(e);
+    }
+    size_t record() {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess || cudaEventRecord(e, stream) != cudaSuccess) ok = false;
+        evs.push_back(e);
+        return evs.size() - 1;
+    }
+    // Starts a segment: a hold kernel long enough for the host to queue the segment behind it.
+    void segment(double hold_us) {
+        launch_hold((long long)(hold_us * 2.1e3), stream);
+        prev = record();
+    }
+    void launched(const char* kernel, cudaStream_t st) override {
+        if (st != stream) return;
+        const size_t e = record();
+        spans.push_back({e, kernel});
+    }
+};
+
+// One substep launched kernel by kernel (eager, no graph) with an event after each kernel.
+// Records are per kernel name, in order of first launch: launches and summed device time.
 int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
     if (dirty) {
         int rc = rebuild();
         if (rc) return rc;
     }
+    const int n = int(sims.size());
+    KernelTimer timer(stream);
+    std::vector<size_t> seg_start;   // span index -> event index that precedes it
+    struct Guard {
+        LaunchLog* old;
+        explicit Guard(LaunchLog* l) : old(g_launch_log) { g_launch_log = l; }
+        ~Guard() { g_launch_log = old; }
+    };
+    cudaError_t e;
+    {
+        Guard g(&timer);
+        // pre-solve kernels (and the whole red-black schedule) in one segment
+        timer.segment(1000.0 + 40.0 * (any_gs ? max_gs_iters : 0));
+        std::vector<std::pair<size_t, size_t>> starts;   // (first span of the segment, its start event)
+        auto mark_segment = [&]() { starts.push_back({timer.spans.size(), timer.prev}); };
+        mark_segment();
+        if ((e = launch_scan(w_chunks, d_sims, n, stream)) != cudaSuccess) return cuda_fail(e, "scan");
+        if ((e = launch_scatter(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "scatter");
+        if ((e = launch_p2g(w_tiles, tile_shape, stream)) != cudaSuccess) return cuda_fail(e, "p2g");
+        if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
+        if (any_gs) {
+            for (uint32_t it = 0; it < max_gs_iters; it++)
+                for (uint32_t parity = 0; parity < 2; parity++)
+                    if ((e = launch_pressure_rb(w_half, parity, it, stream)) != cudaSuccess)
+                        return cuda_fail(e, "pressure");
+        }
+        if (any_pcg && persistent) {
+            if ((e = launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream)) != cudaSuccess)
+                return cuda_fail(e, "pcg solve");
+        } else if (any_pcg) {
+            if (!d_flag) {
+                if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+                if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+            }
+            if ((e = launch_pcg_init(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
+            for (uint32_t guard = 0; guard < 100000; guard++) {
+                if ((e = launch_pcg_any(d_sims, n, d_flag, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+                cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
+                int rc = wait();
+                if (rc) return rc;
+                if (*h_flag == 0) break;
+                timer.segment(1000.0);
+                mark_segment();
+                if ((e = launch_pcg_body(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            }
+            timer.segment(200.0);
+            mark_segment();
+            if ((e = launch_pcg_finish(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
+        }
+        if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
+        if ((e = launch_g2p(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "g2p");
+        int rc = wait();
+        if (rc) return rc;
+        if (!timer.ok) return fail(PXF_ECUDA, "profiler events");
+        // each span starts at the event before it (the segment start for a segment's first kernel)
+        size_t si = 0;
+        for (size_t i = 0; i < timer.spans.size(); i++) {
+            while (si + 1 < starts.size() && starts[si + 1].first <= i) si++;
+            const size_t from = (i == starts[si].first) ? starts[si].second : timer.spans[i - 1].first;
+            seg_start.push_back(from);
+        }
+    }
     struct Rec { const char* name; uint32_t launches; double ms; };
     std::vector<Rec> recs;
-    std::vector<cudaEvent_t> evs;
-    auto ev = [&]() {
-        cudaEvent_t e;
-        cudaEventCreate(&e);
-        cudaEventRecord(e, stream);
-        evs.push_back(e);
-        return evs.size() - 1;
-    };
-    std::vector<std::pair<size_t, size_t>> spans;   // event index pairs per record
-    std::vector<int> owner;
-    auto add = [&](const char* name, size_t a, size_t b) {
+    for (size_t i = 0; i < timer.spans.size(); i++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, timer.evs[seg_start[i]], timer.evs[timer.spans[i].first]);
+        const char* name = timer.spans[i].second;
         int k = -1;
-        for (size_t i = 0; i < recs.size(); i++) if (std::strcmp(recs[i].name, name) == 0) k = int(i);
+        for (size_t j = 0; j < recs.size(); j++) if (std::strcmp(recs[j].name, name) == 0) k = int(j);
         if (k < 0) { recs.push_back({name, 0, 0.0}); k = int(recs.size() - 1); }
         recs[k].launches++;
-        spans.push_back({a, b});
-        owner.push_back(k);
-    };
-    const int n = int(sims.size());
-    cudaError_t e;
-    size_t t0 = ev();
-    if ((e = launch_scan(w_chunks, d_sims, n, stream)) != cudaSuccess) return cuda_fail(e, "scan");
-    size_t t1 = ev(); add("scan+classify", t0, t1);
-    if ((e = launch_scatter(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "scatter");
-    size_t t2 = ev(); add("scatter", t1, t2);
-    if ((e = launch_p2g(w_tiles, tile_shape, stream)) != cudaSuccess) return cuda_fail(e, "p2g");
-    size_t t3 = ev(); add("p2g", t2, t3);
-    if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
-    size_t t4 = ev(); add("divergence", t3, t4);
-    size_t prev = t4;
-    if (any_gs) {
-        for (uint32_t it = 0; it < max_gs_iters; it++)
-            for (uint32_t parity = 0; parity < 2; parity++) {
-                if ((e = launch_pressure_rb(w_half, parity, it, stream)) != cudaSuccess) return cuda_fail(e, "pressure");
-                size_t t = ev(); add("pressure_rb", prev, t); prev = t;
-            }
+        recs[k].ms += ms;
     }
-    if (any_pcg && persistent) {
-        if ((e = launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream)) != cudaSuccess)
-            return cuda_fail(e, "pcg solve");
-        size_t t = ev(); add("pcg_solve_persistent", prev, t); prev = t;
-    } else if (any_pcg) {
-        if (!d_flag) {
-            if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
-            if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
-        }
-        if ((e = launch_pcg_init(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
-        size_t t = ev(); add("pcg_setup+init", prev, t); prev = t;
-        for (uint32_t guard = 0; guard < 100000; guard++) {
-            if ((e = launch_pcg_dir(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t a1 = ev(); add("pcg_dir", prev, a1);
-            if ((e = launch_pcg_update(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t b1 = ev(); add("pcg_update", a1, b1);
-            if ((e = launch_pcg_restart(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t c1 = ev(); add("pcg_restart_check", b1, c1);
-            if ((e = launch_precond(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            size_t d1 = ev(); add(pw.any_mg ? "mg_vcycle" : "jacobi", c1, d1);
-            prev = d1;
-            launch_pcg_any(d_sims, n, d_flag, stream);
-            cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
-            int rc = wait();
-            if (rc) return rc;
-            prev = ev();
-            if (*h_flag == 0) break;
-        }
-        if ((e = launch_pcg_finish(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
-        size_t f = ev(); add("pcg_finish", prev, f); prev = f;
-    }
-    if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
-    size_t t5 = ev(); add("project", prev, t5);
-    if ((e = launch_g2p(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "g2p");
-    size_t t6 = ev(); add("g2p", t5, t6);
-    int rc = wait();
-    if (rc) return rc;
-    for (size_t i = 0; i < spans.size(); i++) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, evs[spans[i].first], evs[spans[i].second]);
-        recs[owner[i]].ms += ms;
-    }
-    for (auto& x : evs) cudaEventDestroy(x);
     for (pxf_sim* s : sims) s->steps_done += 1;
     *count = uint32_t(recs.size());
     for (uint32_t i = 0; i < cap && i < recs.size(); i++) {

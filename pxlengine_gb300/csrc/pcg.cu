@@ -33,6 +33,8 @@
 // (graph-captured, the loop as a conditional while-node) or all inside one persistent cooperative
 // kernel per substep with grid barriers between phases. Barrier waits are bounded: a wait that
 // exceeds its limit raises an error flag that the host reports, and every block returns.
+#include <cstdlib>
+#include <cuda/atomic>
 #include "pxf_device.cuh"
 #include "pxf_kernels.h"
 
@@ -132,6 +134,17 @@ __device__ __forceinline__ void seg(const MgLevel& L, uint32_t chunk, int color,
 
 __device__ __forceinline__ const uint32_t* list_of(const MgLevel& L, uint32_t chunk) {
     return L.list + size_t(chunk) * L.cs;
+}
+
+// Programmatic dependent launch. The kernels of the CG loop are launched so that each may start
+// while the one before it drains. Until dep_wait() returns (the previous kernel has completed and
+// its writes are visible) a kernel reads only what stays fixed during the solve: the simulation
+// descriptors and the cell lists and their counts. Every block waits before it exits, so a
+// kernel completes only after the one before it, and dependents are released only after the
+// wait. Outside such a launch both instructions return at once.
+__device__ __forceinline__ void dep_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 }  // namespace
@@ -259,7 +272,7 @@ __device__ void ph_smooth(const Work& w, int l, int color, int mode) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
-        if (!active(*sp) || sp->precond != 0) continue;
+        if (sp->solver != 1 || sp->precond != 0) continue;
         const MgLevel L = sp->lev[l];
         const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
         const uint32_t chunk = item - w.base[si];
@@ -268,6 +281,8 @@ __device__ void ph_smooth(const Work& w, int l, int color, int mode) {
         uint32_t lo, hi;
         seg(L, chunk, color, lo, hi);
         const uint32_t* __restrict__ lst = list_of(L, chunk);
+        dep_wait();
+        if (ldu(&sp->pcg->done)) continue;
         const uint16_t* __restrict__ info = L.info;
         const float* __restrict__ r = L.r;
         float* __restrict__ z = L.z;
@@ -319,23 +334,29 @@ __device__ void ph_restrict(const Work& w, int l) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
-        if (!active(*sp) || sp->precond != 0) continue;
+        if (sp->solver != 1 || sp->precond != 0) continue;
         const MgLevel F = sp->lev[l], Cc = sp->lev[l + 1];
         const uint32_t nx = uint32_t(F.nx), nxy = uint32_t(F.nx) * uint32_t(F.ny);
         const uint32_t chunk = item - w.base[si];
         uint32_t lo, hi;
         seg(Cc, chunk, 2, lo, hi);
         const uint32_t* lst = list_of(Cc, chunk);
+        dep_wait();
+        if (ldu(&sp->pcg->done)) continue;
         const uint32_t chd = threadIdx.x & 7u;
         const uint32_t per_pass = blockDim.x / 8;
+        // Below the tail, level l+1's first half sweep (red from zero: z = r / cnt) is done here.
+        const bool first_sweep = l + 1 < sp->tail;
         for (uint32_t base = lo; base < hi; base += per_pass) {
             const uint32_t e = base + (threadIdx.x >> 3);
             float res = 0.0f;
             uint32_t P = 0;
+            bool red = false;
             if (e < hi) {
                 P = lst[e];
                 const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
                 const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
+                red = ((I + J + K) & 1) == 0;
                 const int i = 2 * I + int(chd & 1u), j = 2 * J + int((chd >> 1) & 1u), kk = 2 * K + int(chd >> 2);
                 if (i < F.nx && j < F.ny && kk < F.nz) {
                     const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
@@ -353,7 +374,11 @@ __device__ void ph_restrict(const Work& w, int l) {
             res += __shfl_down_sync(0xffffffffu, res, 1, 8);
             res += __shfl_down_sync(0xffffffffu, res, 2, 8);
             res += __shfl_down_sync(0xffffffffu, res, 4, 8);
-            if (e < hi && chd == 0) Cc.r[P] = 0.5f * res;
+            if (e < hi && chd == 0) {
+                const float rc = 0.5f * res;
+                Cc.r[P] = rc;
+                if (first_sweep && red) Cc.z[P] = rc / cnt_of(Cc.info[P]);
+            }
         }
     }
 }
@@ -362,122 +387,152 @@ __device__ void ph_restrict(const Work& w, int l) {
 // Levels tail..nlev-1 (the tail level holds at most kTailCells cells) run as one V-cycle inside
 // one block per simulation, in shared memory. Input r of the tail level, output z of the tail
 // level; when the tail is level 0 the block also writes the level-0 chunk partials of r.z.
+// Each level keeps in shared memory its r and z, a copy of the neighbour record (zero outside
+// the system) and its system cells as one list, red cells first, gathered from the level's
+// global per-chunk lists. A cell's update reads only the other colour, so the order in which a
+// sweep visits its cells changes no result.
 struct TailLevel {
     int nx, ny, nz;
     uint32_t nc;
     float* r;
     float* z;
     uint16_t* info;
+    uint16_t* list;      // system cells: red [0, nred), black [nred, nsys)
+    uint32_t nred, nsys;
 };
 
-__device__ void tail_smooth(const TailLevel& L, const MgLevel& G, uint32_t color, int mode, const TailLevel* C) {
-    const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
-    const uint32_t nch = (L.nc + G.cs - 1) / G.cs;
-    for (uint32_t ch = 0; ch < nch; ch++) {
-        uint32_t lo, hi;
-        seg(G, ch, int(color), lo, hi);
-        const uint32_t* lst = list_of(G, ch);
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const uint32_t c = __ldcg(lst + e);
-            const uint32_t inf = L.info[c];
-            float sum = L.r[c];
-            if (mode == 2) {
-                const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
+constexpr uint32_t kTailMaxChunks = 64;   // list chunks per tail level (kTailCells / kCoarseChunk = 32)
+
+__device__ void tail_smooth(const TailLevel& L, uint32_t color, int mode, const TailLevel* C) {
+    const int nx = L.nx, ny = L.ny, nxy = L.nx * L.ny;
+    const int off[6] = {-1, 1, -nx, nx, -nxy, nxy};
+    const uint16_t* lst = color ? L.list + L.nred : L.list;
+    const uint32_t n = color ? L.nsys - L.nred : L.nred;
+    for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+        const int c = int(lst[e]);
+        const uint32_t inf = L.info[c];
+        float sum = L.r[c];
+        if (mode == 2) {
+            const int i = c % nx, j = (c / nx) % ny, kk = c / nxy;
 #pragma unroll
-                for (int q = 0; q < 6; q++) {
-                    if (!(inf & (1u << q))) continue;
-                    const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
-                    const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
-                    const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
-                    const uint32_t n = uint32_t(int(c) + dx + dy * int(nx) + dz * int(nxy));
-                    float zn = L.z[n];
-                    const uint32_t P = (uint32_t(int(i) + dx) >> 1) + uint32_t(C->nx) * ((uint32_t(int(j) + dy) >> 1) +
-                                       uint32_t(C->ny) * (uint32_t(int(kk) + dz) >> 1));
-                    if (in_system(C->info[P])) zn += C->z[P];
-                    sum += zn;
-                }
-            } else if (mode != 1) {
-#pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (inf & (1u << q)) sum += L.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+            for (int q = 0; q < 6; q++) {
+                if (!(inf & (1u << q))) continue;
+                const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                float zn = L.z[c + off[q]];
+                const uint32_t P = uint32_t((i + dx) >> 1) + uint32_t(C->nx) * (uint32_t((j + dy) >> 1) +
+                                   uint32_t(C->ny) * uint32_t((kk + dz) >> 1));
+                if (C->info[P]) zn += C->z[P];
+                sum += zn;
             }
-            L.z[c] = sum / cnt_of(inf);
+        } else if (mode != 1) {
+#pragma unroll
+            for (int q = 0; q < 6; q++)
+                if (inf & (1u << q)) sum += L.z[c + off[q]];
         }
+        L.z[c] = sum / cnt_of(inf);
     }
     __syncthreads();
 }
 
-__device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc, const MgLevel& GC) {
-    const uint32_t nx = uint32_t(F.nx), nxy = uint32_t(F.nx) * uint32_t(F.ny);
-    const uint32_t nch = (Cc.nc + GC.cs - 1) / GC.cs;
-    for (uint32_t ch = 0; ch < nch; ch++) {
-        uint32_t lo, hi;
-        seg(GC, ch, 2, lo, hi);
-        const uint32_t* lst = list_of(GC, ch);
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const uint32_t P = __ldcg(lst + e);
-            const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
-            const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
-            float sum = 0.0f;
+__device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc) {
+    const int nx = F.nx, nxy = F.nx * F.ny;
+    const int off[6] = {-1, 1, -nx, nx, -nxy, nxy};
+    const uint32_t cnx = uint32_t(Cc.nx), cnxy = uint32_t(Cc.nx) * uint32_t(Cc.ny);
+    for (uint32_t e = threadIdx.x; e < Cc.nsys; e += blockDim.x) {
+        const uint32_t P = Cc.list[e];
+        const int I = int(P % cnx), J = int((P / cnx) % uint32_t(Cc.ny)), K = int(P / cnxy);
+        float sum = 0.0f;
 #pragma unroll
-            for (int chd = 0; chd < 8; chd++) {
-                const int i = 2 * I + (chd & 1), j = 2 * J + ((chd >> 1) & 1), kk = 2 * K + (chd >> 2);
-                if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
-                const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
-                const uint32_t inf = F.info[c];
-                if (!in_system(inf)) continue;
-                float az = cnt_of(inf) * F.z[c];
+        for (int chd = 0; chd < 8; chd++) {
+            const int i = 2 * I + (chd & 1), j = 2 * J + ((chd >> 1) & 1), kk = 2 * K + (chd >> 2);
+            if (i >= F.nx || j >= F.ny || kk >= F.nz) continue;
+            const int c = i + nx * j + nxy * kk;
+            const uint32_t inf = F.info[c];
+            if (!inf) continue;
+            float az = cnt_of(inf) * F.z[c];
 #pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
-                sum += F.r[c] - az;
-            }
-            Cc.r[P] = 0.5f * sum;
+            for (int q = 0; q < 6; q++)
+                if (inf & (1u << q)) az -= F.z[c + off[q]];
+            sum += F.r[c] - az;
         }
+        Cc.r[P] = 0.5f * sum;
     }
     __syncthreads();
 }
 
 __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
     __shared__ double sh[32];
+    __shared__ uint32_t cr[kTailMaxChunks], cb[kTailMaxChunks], orr[kTailMaxChunks], obb[kTailMaxChunks];
+    __shared__ uint32_t tot[2];
     for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
         const SimDev* sp = sims + si;
-        if (sp->solver != 1 || sp->precond != 0 || __ldcg(&sp->pcg->done)) continue;
+        if (sp->solver != 1 || sp->precond != 0) continue;
         const int T = sp->tail, NL = sp->nlev;
         TailLevel lv[kMaxLevels];
-        // shared layout per level: r, z (float), info (u16, padded to floats)
         float* base = tsm;
         for (int l = T; l < NL; l++) {
             const MgLevel g = sp->lev[l];
-            lv[l].nx = g.nx; lv[l].ny = g.ny; lv[l].nz = g.nz; lv[l].nc = g.nc;
-            lv[l].r = base;
-            lv[l].z = base + g.nc;
-            lv[l].info = reinterpret_cast<uint16_t*>(base + 2 * g.nc);
-            base += 2 * g.nc + (g.nc + 1) / 2;
-            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[l].info[c] = __ldcg(g.info + c);
+            TailLevel& t = lv[l];
+            t.nx = g.nx; t.ny = g.ny; t.nz = g.nz; t.nc = g.nc;
+            t.r = base;
+            t.z = base + g.nc;
+            t.info = reinterpret_cast<uint16_t*>(base + 2 * g.nc);
+            t.list = t.info + g.nc;
+            base += tail_level_floats(g.nc);
+            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) {
+                const uint32_t inf = __ldcg(g.info + c);
+                t.info[c] = in_system(inf) ? uint16_t(inf) : uint16_t(0);
+            }
+            // gather the per-chunk red / black lists into one list
+            const uint32_t nch = (g.nc + g.cs - 1) / g.cs;
+            for (uint32_t k = threadIdx.x; k < nch; k += blockDim.x) {
+                cr[k] = __ldcg(g.lcnt + 2 * k);
+                cb[k] = __ldcg(g.lcnt + 2 * k + 1);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t a = 0, b = 0;
+                for (uint32_t k = 0; k < nch; k++) { orr[k] = a; a += cr[k]; }
+                for (uint32_t k = 0; k < nch; k++) { obb[k] = a + b; b += cb[k]; }
+                tot[0] = a;
+                tot[1] = a + b;
+            }
+            __syncthreads();
+            t.nred = tot[0];
+            t.nsys = tot[1];
+            for (uint32_t e = threadIdx.x; e < nch * g.cs; e += blockDim.x) {
+                const uint32_t k = e / g.cs, m = e - k * g.cs;
+                if (m < cr[k]) t.list[orr[k] + m] = uint16_t(__ldcg(g.list + e));
+                else if (m < cr[k] + cb[k]) t.list[obb[k] + m - cr[k]] = uint16_t(__ldcg(g.list + e));
+            }
+            __syncthreads();
         }
-        {
-            const MgLevel g = sp->lev[T];
-            for (uint32_t c = threadIdx.x; c < g.nc; c += blockDim.x) lv[T].r[c] = __ldcg(g.r + c);
+        // everything above is fixed during the solve; r is the previous kernel's output
+        dep_wait();
+        if (__ldcg(&sp->pcg->done)) {
+            __syncthreads();
+            continue;
         }
+        for (uint32_t c = threadIdx.x; c < lv[T].nc; c += blockDim.x) lv[T].r[c] = __ldcg(sp->lev[T].r + c);
         __syncthreads();
         for (int l = T; l + 1 < NL; l++) {
-            tail_smooth(lv[l], sp->lev[l], 0, 1, nullptr);
-            tail_smooth(lv[l], sp->lev[l], 1, 0, nullptr);
-            tail_restrict(lv[l], lv[l + 1], sp->lev[l + 1]);
+            tail_smooth(lv[l], 0, 1, nullptr);
+            tail_smooth(lv[l], 1, 0, nullptr);
+            tail_restrict(lv[l], lv[l + 1]);
         }
         {
             const TailLevel& Lc = lv[NL - 1];
-            const MgLevel Gc = sp->lev[NL - 1];
             for (uint32_t c = threadIdx.x; c < Lc.nc; c += blockDim.x) Lc.z[c] = 0.0f;
             __syncthreads();
             const uint32_t it = sp->coarse_iters;
-            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, Gc, 0, 0, nullptr); tail_smooth(Lc, Gc, 1, 0, nullptr); }
-            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, Gc, 1, 0, nullptr); tail_smooth(Lc, Gc, 0, 0, nullptr); }
+            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, 0, 0, nullptr); tail_smooth(Lc, 1, 0, nullptr); }
+            for (uint32_t h = 0; h < it; h++) { tail_smooth(Lc, 1, 0, nullptr); tail_smooth(Lc, 0, 0, nullptr); }
         }
         for (int l = NL - 2; l >= T; l--) {
-            tail_smooth(lv[l], sp->lev[l], 1, 2, &lv[l + 1]);
-            tail_smooth(lv[l], sp->lev[l], 0, 0, nullptr);
+            tail_smooth(lv[l], 1, 2, &lv[l + 1]);
+            tail_smooth(lv[l], 0, 0, nullptr);
         }
         {
             const MgLevel g = sp->lev[T];
@@ -490,7 +545,7 @@ __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
                 DF acc{0.f, 0.f};
                 const uint32_t end = min((ch + 1) * kScanChunk, sp->nc);
                 for (uint32_t c = ch * kScanChunk + threadIdx.x; c < end; c += blockDim.x)
-                    if (in_system(lv[0].info[c])) acc = df_add(acc, two_prod(lv[0].r[c], lv[0].z[c]));
+                    if (lv[0].info[c]) acc = df_add(acc, two_prod(lv[0].r[c], lv[0].z[c]));
                 const double t = block_sum(acc, sh);
                 if (threadIdx.x == 0) sp->partial[ch] = t;
             }
@@ -505,12 +560,14 @@ __device__ void ph_jacobi(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (!active(s) || s.precond != 1) continue;
+        if (s.solver != 1 || s.precond != 1) continue;
         const uint32_t chunk = item - w.base[si];
         DF acc{0.f, 0.f};
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
         const uint32_t* lst = list_of(s.lev[0], chunk);
+        dep_wait();
+        if (ldu(&s.pcg->done)) continue;
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
@@ -550,12 +607,14 @@ __device__ void ph_widen(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (!active(s) || !ldu(&s.pcg->restart_now)) continue;
-        const bool zero = ldu(&s.pcg->zero_x) != 0;
+        if (s.solver != 1) continue;
         const uint32_t chunk = item - w.base[si];
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
         const uint32_t* lst = list_of(s.lev[0], chunk);
+        dep_wait();
+        if (ldu(&s.pcg->done) || !ldu(&s.pcg->restart_now)) continue;
+        const bool zero = ldu(&s.pcg->zero_x) != 0;
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             if (zero) {
@@ -575,13 +634,17 @@ __device__ void ph_resid(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (!active(s) || !ldu(&s.pcg->restart_now) || ldu(&s.pcg->zero_x)) continue;
+        if (s.solver != 1) continue;
         const uint32_t chunk = item - w.base[si];
         const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         double rr = 0;
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
         const uint32_t* lst = list_of(s.lev[0], chunk);
+        dep_wait();
+        if (ldu(&s.pcg->done) || !ldu(&s.pcg->restart_now) || ldu(&s.pcg->zero_x)) continue;
+        // as in ph_update: the level-0 red half sweep from zero
+        const uint32_t nred = (s.precond == 0 && s.tail > 0) ? __ldcg(s.lev[0].lcnt + 2 * chunk) : 0u;
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             const uint32_t inf = s.info[c];
@@ -590,7 +653,9 @@ __device__ void ph_resid(const Work& w) {
             for (int q = 0; q < 6; q++)
                 if (inf & (1u << q)) ax -= s.x64[int64_t(c) + nbr(q, nx, nxy)];
             const double rd = -double(rhs_of(s, c)) - ax;
-            s.r[c] = float(rd);
+            const float rf = float(rd);
+            s.r[c] = rf;
+            if (e < nred) s.lev[0].z[c] = rf / cnt_of(inf);
             rr += rd * rd;
         }
 #pragma unroll
@@ -613,8 +678,12 @@ __device__ void ph_dir(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (!active(s)) continue;
+        if (s.solver != 1) continue;
         const uint32_t chunk = item - w.base[si];
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        dep_wait();
+        if (ldu(&s.pcg->done)) continue;
         const PcgState* st = s.pcg;
         const uint32_t pbuf = ldu(&st->pbuf);
         const float* __restrict__ pold = pbuf ? s.p1 : s.p0;
@@ -626,8 +695,6 @@ __device__ void ph_dir(const Work& w) {
         const float beta = fresh ? 0.0f : float(ldd(&st->beta));
         const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         DF acc{0.f, 0.f};
-        uint32_t lo, hi;
-        seg(s.lev[0], chunk, 2, lo, hi);
         const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
 #pragma unroll 2
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
@@ -657,8 +724,14 @@ __device__ void ph_update(const Work& w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
-        if (!active(s)) continue;
+        if (s.solver != 1) continue;
         const uint32_t chunk = item - w.base[si];
+        uint32_t lo, hi;
+        seg(s.lev[0], chunk, 2, lo, hi);
+        // The V-cycle's first half sweep on level 0 (red from zero: z = r / cnt) is done here.
+        const uint32_t nred = (s.precond == 0 && s.tail > 0) ? __ldcg(s.lev[0].lcnt + 2 * chunk) : 0u;
+        dep_wait();
+        if (ldu(&s.pcg->done)) continue;
         const PcgState* st = s.pcg;
         const float* __restrict__ p = ldu(&st->pbuf) ? s.p1 : s.p0;
         float2* __restrict__ x2 = s.x2;
@@ -667,9 +740,8 @@ __device__ void ph_update(const Work& w) {
         const float ah = ldf(&st->alpha_hi), al = ldf(&st->alpha_lo);
         const float af = float(ldd(&st->alpha));
         DF acc{0.f, 0.f};
-        uint32_t lo, hi;
-        seg(s.lev[0], chunk, 2, lo, hi);
         const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
+        float* __restrict__ z = s.lev[0].z;
 #pragma unroll 2
         for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
@@ -681,6 +753,7 @@ __device__ void ph_update(const Work& w) {
             x2[c] = make_float2(xn.hi, xn.lo);
             const float rn = r[c] - af * Ap[c];
             r[c] = rn;
+            if (e < nred) z[c] = rn / cnt_of(s.info[c]);
             acc = df_add(acc, two_prod(rn, rn));
         }
         const double t = block_sum(acc, sh);
@@ -713,6 +786,7 @@ __device__ void ph_finish(const Work& w) {
 // 4: after |r|^2
 __device__ void ph_ctl(const SimDev* sims, int n_sims, int phase) {
     __shared__ double sh[32];
+    dep_wait();
     for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
         const SimDev& s = sims[si];
         if (s.solver != 1) continue;
@@ -801,18 +875,19 @@ __device__ __forceinline__ bool any_restart(const SimDev* sims, int n_sims) {
 __global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) { ph_cell_lists(w, l); }
 __global__ void __launch_bounds__(THREADS) k_mg_coarsen(Work w, int l) { ph_coarsen(w, l); }
 __global__ void __launch_bounds__(THREADS) k_mg_info(Work w, int l) { ph_info(w, l); }
-__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode) { ph_smooth(w, l, color, mode); }
-__global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) { ph_restrict(w, l); }
-__global__ void __launch_bounds__(1024) k_mg_tail(const SimDev* sims, int n_sims) {
+__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode) { ph_smooth(w, l, color, mode); dep_wait(); }
+__global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) { ph_restrict(w, l); dep_wait(); }
+__global__ void __launch_bounds__(1024, 1) k_mg_tail(const SimDev* sims, int n_sims) {
     extern __shared__ float tsm[];
     ph_tail(sims, n_sims, tsm);
+    dep_wait();
 }
-__global__ void __launch_bounds__(THREADS) k_jacobi(Work w) { ph_jacobi(w); }
+__global__ void __launch_bounds__(THREADS) k_jacobi(Work w) { ph_jacobi(w); dep_wait(); }
 __global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) { ph_init(w); }
-__global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) { ph_widen(w); }
-__global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) { ph_resid(w); }
-__global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) { ph_dir(w); }
-__global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) { ph_update(w); }
+__global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) { ph_widen(w); dep_wait(); }
+__global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) { ph_resid(w); dep_wait(); }
+__global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) { ph_dir(w); dep_wait(); }
+__global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) { ph_update(w); dep_wait(); }
 __global__ void __launch_bounds__(THREADS) k_pcg_finish(Work w) { ph_finish(w); }
 __global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_sims, int phase) { ph_ctl(sims, n_sims, phase); }
 
@@ -832,31 +907,28 @@ __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
 }
 
 // ============================================================================ persistent solve
-// Grid barrier with a bounded wait: arrive on a counter, the last block advances the generation;
-// the others poll it with a cycle limit. A timed-out wait sets `err`; every block then leaves.
+// Sense-reversing grid barrier on one word: block 0 adds 2^31 - (blocks - 1), every other block
+// adds 1, so the word's top bit flips exactly when the last block arrives and its low 31 bits
+// return to zero. Each block waits for the flip, at most kBarrierCycles; a block that gives up
+// sets `err` and every block leaves the solve at its next barrier. The launch zeroes the whole
+// GridBar, so a barrier left half-passed by an abandoned launch never reaches the next one.
 __device__ __forceinline__ bool grid_sync(GridBar* b) {
     __shared__ int bad;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned g = __ldcg(&b->gen);
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> word(b->count), err(b->err);
+        const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
         __threadfence();
-        const unsigned arrived = atomicAdd(&b->count, 1u);
-        if (arrived == gridDim.x - 1) {
-            b->count = 0;
-            __threadfence();
-            atomicAdd(&b->gen, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (__ldcg(&b->gen) == g) {
-                if (__ldcg(&b->err) || clock64() - t0 > kBarrierCycles) {
-                    atomicExch(&b->err, 1u);
-                    break;
-                }
-                __nanosleep(32);
+        const unsigned old = word.fetch_add(inc, cuda::memory_order_relaxed);
+        const long long t0 = clock64();
+        while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
+            if (err.load(cuda::memory_order_relaxed) || clock64() - t0 > kBarrierCycles) {
+                err.store(1u, cuda::memory_order_relaxed);
+                break;
             }
         }
         __threadfence();
-        bad = __ldcg(&b->err) != 0;
+        bad = err.load(cuda::memory_order_relaxed) != 0u;
     }
     __syncthreads();
     return !bad;
@@ -880,8 +952,6 @@ __device__ bool solve_precond(const SolveArgs& a, float* tsm) {
     if (pw.any_mg) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
-            ph_smooth(pw.level[l], l, 0, 1);
-            if (!grid_sync(a.bar)) return false;
             ph_smooth(pw.level[l], l, 1, 0);
             if (!grid_sync(a.bar)) return false;
             ph_restrict(pw.coarse[l], l);
@@ -949,10 +1019,9 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
 }
 
 // ============================================================================ launchers
-static unsigned grid_of(uint32_t total) {
-    const uint32_t cap = uint32_t(sm_count() * grid_cap_per_sm());
-    return total < cap ? (total ? total : 1u) : cap;
-}
+// One block per work item (chunk): chunks of the air exit at once, and the block scheduler hands
+// the rest to whichever SM frees first.
+static unsigned grid_of(uint32_t total) { return total ? total : 1u; }
 
 static inline Work mkw(const StageWork& sw) {
     Work w;
@@ -963,8 +1032,28 @@ static inline Work mkw(const StageWork& sw) {
     return w;
 }
 
+// Launch of a CG-loop kernel with programmatic stream serialization (it may start while the
+// kernel before it drains; see dep_wait). PXF_PDL=0 launches them in plain stream order.
+template <typename... KArgs, typename... Args>
+static void launch_dep(const char* name, void (*k)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                       cudaStream_t st, Args... args) {
+    static const bool pdl = [] { const char* v = std::getenv("PXF_PDL"); return !(v && v[0] == '0'); }();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, KArgs(args)...);
+    note_launch(name, st);
+}
+
 static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st) {
-    k_pcg_ctl<<<pw.n_sims, THREADS, 0, st>>>(pw.sims, pw.n_sims, phase);
+    launch_dep("k_pcg_ctl", k_pcg_ctl, pw.n_sims, THREADS, 0, st, pw.sims, pw.n_sims, phase);
     return cudaGetLastError();
 }
 
@@ -975,56 +1064,58 @@ cudaError_t mg_tail_attr(size_t smem) {
 }
 
 cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
-    k_cell_lists<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks), 0);
+    k_cell_lists<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks), 0); note_launch("k_cell_lists", st);
     for (int l = 0; l + 1 < pw.setup_levels; l++) {
         if (!pw.setup[l].total) continue;
-        k_mg_coarsen<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l);
-        k_mg_info<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l);
-        k_cell_lists<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l + 1);
+        k_mg_coarsen<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l); note_launch("k_mg_coarsen", st);
+        k_mg_info<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l); note_launch("k_mg_info", st);
+        k_cell_lists<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l + 1); note_launch("k_cell_lists", st);
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
-    if (pw.any_jacobi) k_jacobi<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    if (pw.any_jacobi) {
+        launch_dep("k_jacobi", k_jacobi, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
+    }
     if (pw.any_mg) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
-            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 0, 1);
-            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 1, 0);
-            k_mg_restrict<<<grid_of(pw.coarse[l].total), THREADS, 0, st>>>(mkw(pw.coarse[l]), l);
+            // (the red half sweep from zero ran in the kernel that produced this level's r)
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_of(pw.level[l].total), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0);
+            launch_dep("k_mg_restrict", k_mg_restrict, grid_of(pw.coarse[l].total), THREADS, 0, st, mkw(pw.coarse[l]), l);
         }
-        k_mg_tail<<<pw.n_sims, 1024, pw.tail_smem, st>>>(pw.sims, pw.n_sims);
+        launch_dep("k_mg_tail", k_mg_tail, pw.n_sims, 1024, pw.tail_smem, st, pw.sims, pw.n_sims);
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
-            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 1, 2);
-            k_mg_smooth<<<grid_of(pw.level[l].total), THREADS, 0, st>>>(mkw(pw.level[l]), l, 0, l == 0 ? 3 : 0);
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_of(pw.level[l].total), THREADS, 0, st, mkw(pw.level[l]), l, 1, 2);
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_of(pw.level[l].total), THREADS, 0, st, mkw(pw.level[l]), l, 0, l == 0 ? 3 : 0);
         }
     }
     return ctl(pw, 2, st);
 }
 
 cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st) {
-    k_pcg_widen<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
-    k_pcg_resid<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    launch_dep("k_pcg_widen", k_pcg_widen, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
+    launch_dep("k_pcg_resid", k_pcg_resid, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
     return ctl(pw, 1, st);
 }
 
 cudaError_t launch_pcg_init(const PcgWork& pw, cudaStream_t st) {
     launch_mg_setup(pw, st);
-    k_pcg_init<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    k_pcg_init<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks)); note_launch("k_pcg_init", st);
     ctl(pw, 0, st);
     launch_pcg_restart(pw, st);
     return launch_precond(pw, st);
 }
 
 cudaError_t launch_pcg_dir(const PcgWork& pw, cudaStream_t st) {
-    k_pcg_dir<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    launch_dep("k_pcg_dir", k_pcg_dir, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
     return ctl(pw, 3, st);
 }
 
 cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st) {
-    k_pcg_update<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    launch_dep("k_pcg_update", k_pcg_update, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
     return ctl(pw, 4, st);
 }
 
@@ -1036,22 +1127,22 @@ cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st) {
 }
 
 cudaError_t launch_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {
-    k_pcg_restart_cond<<<1, 32, 0, st>>>(sims, n_sims, h);
+    k_pcg_restart_cond<<<1, 32, 0, st>>>(sims, n_sims, h); note_launch("k_pcg_restart_cond", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {
-    k_pcg_cond<<<1, 32, 0, st>>>(sims, n_sims, h);
+    k_pcg_cond<<<1, 32, 0, st>>>(sims, n_sims, h); note_launch("k_pcg_cond", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaStream_t st) {
-    k_pcg_any<<<1, 32, 0, st>>>(sims, n_sims, flag);
+    k_pcg_any<<<1, 32, 0, st>>>(sims, n_sims, flag); note_launch("k_pcg_any", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st) {
-    k_pcg_finish<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks));
+    k_pcg_finish<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks)); note_launch("k_pcg_finish", st);
     return cudaGetLastError();
 }
 
@@ -1064,7 +1155,7 @@ int pcg_solve_grid(size_t smem) {
 }
 
 cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(&bar->err, 0, sizeof(uint32_t), st);
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
     SolveArgs a;
     a.pw = pw;
@@ -1080,7 +1171,9 @@ cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_pcg_solve, a);
+    e = cudaLaunchKernelEx(&cfg, k_pcg_solve, a);
+    note_launch("k_pcg_solve", st);
+    return e;
 }
 
 }  // namespace pxf

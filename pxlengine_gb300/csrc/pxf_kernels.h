@@ -15,6 +15,22 @@ constexpr uint32_t kElemItem = 256;       // elements per item of the per-elemen
 constexpr int kMaxLevelsK = 12;           // multigrid levels (kMaxLevels in pxf_device.cuh)
 
 int sm_count();
+
+// Kernel launches issued by the calling host thread (eager or into a stream capture), and an
+// optional per-thread log that the substep profiler installs to time every kernel separately.
+struct LaunchLog {
+    virtual void launched(const char* kernel, cudaStream_t st) = 0;
+};
+extern thread_local uint64_t g_kernel_launches;
+extern thread_local LaunchLog* g_launch_log;
+inline void note_launch(const char* kernel, cudaStream_t st) {
+    ++g_kernel_launches;
+    if (g_launch_log) g_launch_log->launched(kernel, st);
+}
+// A one-warp kernel that busy-waits `cycles` SM clocks (bounded by construction). The profiler
+// puts one ahead of each eagerly launched segment so the host has queued the segment before
+// the GPU reaches it, and the gaps between events are device time, not host launch time.
+cudaError_t launch_hold(long long cycles, cudaStream_t st);
 int grid_cap_per_sm();
 void p2g_shape(int shape, int out[3]);
 extern const int kNumP2GShapes;
@@ -46,14 +62,17 @@ struct PcgWork {
     size_t tail_smem = 0;               // dynamic shared memory of the tail kernel
 };
 
-constexpr uint32_t kTailCells = 1024;   // the shared-memory tail starts at the first level this small
+constexpr uint32_t kTailCells = 8192;   // the shared-memory tail starts at the first level this small
+static_assert(kTailCells <= 65536, "tail lists hold cell indices as 16-bit values");
+// Shared-memory floats a tail level of nc cells takes: r, z (float), neighbour record and list (u16).
+__host__ __device__ constexpr uint32_t tail_level_floats(uint32_t nc) { return 3 * nc; }
 constexpr uint32_t kCoarseChunk = 256;  // list chunk of the levels below level 0
 cudaError_t mg_tail_attr(size_t smem);
 
-// Grid barrier of the persistent solve (device memory, zero-initialised).
+// Grid barrier of the persistent solve (device memory, zeroed at every launch).
 struct GridBar {
-    unsigned count;
-    unsigned gen;
+    unsigned count;    // arrival word: top bit = barrier phase, low bits = arrivals
+    unsigned gen;      // unused
     unsigned err;      // set when a wait exceeded kBarrierCycles
     unsigned pad;
 };

@@ -10,6 +10,7 @@
 #include <cstdint>
 
 #include "pxf_device.cuh"
+#include "pxf_kernels.h"
 #include "seed.h"
 
 namespace pxf {
@@ -144,7 +145,7 @@ cudaError_t launch_seed(const SeedPlan& plan, float4* pos, float4* vel, float4* 
         if (a.p_end <= a.p_begin) continue;
         const uint64_t blocks = (a.p_end - a.p_begin + 255) / 256;
         const unsigned grid = blocks < 65535ull * 16 ? unsigned(blocks) : 65535u * 16;
-        k_seed<<<grid, 256, 0, st>>>(a, pos, vel, pos0, vel0);
+        k_seed<<<grid, 256, 0, st>>>(a, pos, vel, pos0, vel0); note_launch("k_seed", st);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

@@ -630,6 +630,20 @@ __global__ void k_counts_from_start(SimDev s, uint32_t* __restrict__ out) {
 }
 
 // ------------------------------------------------------------------ launchers
+thread_local uint64_t g_kernel_launches = 0;
+thread_local LaunchLog* g_launch_log = nullptr;
+
+__global__ void k_hold(long long cycles) {
+    const long long t0 = clock64();
+    while (clock64() - t0 < cycles) {
+    }
+}
+
+cudaError_t launch_hold(long long cycles, cudaStream_t st) {
+    k_hold<<<1, 32, 0, st>>>(cycles);
+    return cudaGetLastError();
+}
+
 static int g_sm_count = 0;
 
 int sm_count() {
@@ -678,7 +692,10 @@ static cudaError_t launch_p2g_t(const StageWork& sw, cudaStream_t st) {
     if (per_sm < 1) per_sm = 1;
     static const int strided = [] { const char* v = std::getenv("PXF_P2G_STRIDED"); return v ? std::atoi(v) : 1; }();
     static const int pack = [] { const char* v = std::getenv("PXF_P2G_PACKED"); return v ? std::atoi(v) : 0; }();
-    k_p2g<TX, TY, TZ><<<grid_for(sw.total, per_sm), 256, T::SMEM, st>>>(mk(sw), strided, pack);
+    // One block per tile: tiles of the liquid hold most of the work and those of the air none, so
+    // the block scheduler's dynamic assignment balances the SMs (a grid-strided loop would not).
+    (void)per_sm;
+    k_p2g<TX, TY, TZ><<<sw.total ? sw.total : 1u, 256, T::SMEM, st>>>(mk(sw), strided, pack); note_launch("k_p2g", st);
     return cudaGetLastError();
 }
 
@@ -703,54 +720,54 @@ cudaError_t launch_p2g(const StageWork& sw, int shape, cudaStream_t st) {
 }
 
 cudaError_t launch_scan(const StageWork& chunks, const SimDev* sims, int n_sims, cudaStream_t st) {
-    k_scan_chunks<<<grid_for(chunks.total, 8), 256, 0, st>>>(mk(chunks));
-    k_scan_sims<<<n_sims, 1024, 0, st>>>(sims, n_sims);
-    k_scan_apply<<<grid_for(chunks.total, 8), 256, 0, st>>>(mk(chunks));
+    k_scan_chunks<<<grid_for(chunks.total, 8), 256, 0, st>>>(mk(chunks)); note_launch("k_scan_chunks", st);
+    k_scan_sims<<<n_sims, 1024, 0, st>>>(sims, n_sims); note_launch("k_scan_sims", st);
+    k_scan_apply<<<grid_for(chunks.total, 8), 256, 0, st>>>(mk(chunks)); note_launch("k_scan_apply", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scatter(const StageWork& parts, cudaStream_t st) {
-    k_scatter<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts));
+    k_scatter<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts)); note_launch("k_scatter", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bin(const StageWork& parts, cudaStream_t st) {
-    k_bin<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts));
+    k_bin<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts)); note_launch("k_bin", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st) {
-    k_divergence<<<grid_for(cells.total, 8), 256, 0, st>>>(mk(cells));
+    k_divergence<<<grid_for(cells.total, 8), 256, 0, st>>>(mk(cells)); note_launch("k_divergence", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st) {
-    k_pressure_rb<<<grid_for(half_cells.total, 8), 256, 0, st>>>(mk(half_cells), parity, it);
+    k_pressure_rb<<<grid_for(half_cells.total, 8), 256, 0, st>>>(mk(half_cells), parity, it); note_launch("k_pressure_rb", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_project(const StageWork& faces, cudaStream_t st) {
-    k_project<<<grid_for(faces.total, 8), 256, 0, st>>>(mk(faces));
+    k_project<<<grid_for(faces.total, 8), 256, 0, st>>>(mk(faces)); note_launch("k_project", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_g2p(const StageWork& parts, cudaStream_t st) {
-    k_g2p<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts));
+    k_g2p<<<grid_for(parts.total, 8), 256, 0, st>>>(mk(parts)); note_launch("k_g2p", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_gather_aos(const SimDev& s, float4* out, cudaStream_t st) {
-    k_gather_aos<<<grid_for((s.np + 255) / 256, 8), 256, 0, st>>>(s, out);
+    k_gather_aos<<<grid_for((s.np + 255) / 256, 8), 256, 0, st>>>(s, out); note_launch("k_gather_aos", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scatter_aos(const SimDev& s, const float4* in, cudaStream_t st) {
-    k_scatter_aos<<<grid_for((s.np + 255) / 256, 8), 256, 0, st>>>(s, in);
+    k_scatter_aos<<<grid_for((s.np + 255) / 256, 8), 256, 0, st>>>(s, in); note_launch("k_scatter_aos", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_counts_from_start(const SimDev& s, uint32_t* out, cudaStream_t st) {
-    k_counts_from_start<<<grid_for((s.nc + 255) / 256, 8), 256, 0, st>>>(s, out);
+    k_counts_from_start<<<grid_for((s.nc + 255) / 256, 8), 256, 0, st>>>(s, out); note_launch("k_counts_from_start", st);
     return cudaGetLastError();
 }
 

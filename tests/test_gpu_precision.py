@@ -69,3 +69,35 @@ def test_pcg_iteration_cap_reports_status(lib):
         s.step(1)
         it, rel, status = s.solver_stats()
         assert status == 1 and it == 5 and rel > 1e-12
+
+
+@pytest.mark.parametrize("precond", ["mg", "jacobi"])
+def test_persistent_solve_matches_graph_loop(lib, monkeypatch, precond):
+    """The persistent cooperative solve (one launch, grid barriers) runs the same phases over the
+    same chunks as the graph of kernels, so both give identical bits."""
+    f = dam(res=48, ppc=4)
+    opts = P.make_options(solver="pcg", rtol=PCG_RTOL, max_iter=4000, restart=50, precond=precond)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("PXF_PCG_PERSISTENT", mode)
+        with P.FluidState(f, fps=15.0, options=opts) as s:
+            s.step(3)
+            out[mode] = (s.read_particles(), s.read_grid("pressure64"), s.solver_stats())
+    assert out["0"][2][2] == 0 and out["1"][2][2] == 0
+    assert out["0"][2][0] == out["1"][2][0]
+    assert np.array_equal(out["0"][0], out["1"][0])
+    assert np.array_equal(out["0"][1], out["1"][1])
+
+
+def test_precision_solve_is_deterministic(lib):
+    """Fixed-order reductions and overlapped (programmatic) launches: two runs give the same bits."""
+    f = dam(res=96, ppc=4)
+    opts = P.make_options(solver="pcg", rtol=PCG_RTOL, max_iter=4000, restart=50)
+    out = []
+    for _ in range(2):
+        with P.FluidState(f, fps=15.0, options=opts) as s:
+            s.step(6)
+            out.append((s.read_particles(), s.read_grid("pressure64"), s.solver_stats()))
+    assert out[0][2] == out[1][2]
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
