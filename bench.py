@@ -159,7 +159,8 @@ def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1):
     dt = oracle.dt_for(cfg["fps"], cfg["substeps"])
     s = oracle.OracleSim(dims, h, dt, 0.95, list(cfg["bounds"][0]), [0, -9.81, 0], cfg["iterations"], p)
     if cfg["solver"] == "pcg":
-        s.set_pressure("pcg", rtol=1e-6, max_iter=4000, restart=50)
+        # the same algorithm as the GPU path: multigrid-preconditioned CG, FP64 dots and restarts
+        s.set_pressure("mgpcg", rtol=1e-6, max_iter=4000, restart=50)
     for _ in range(warmup):
         s.step(sample_substeps)
     t0 = time.perf_counter()
@@ -171,24 +172,173 @@ def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1):
             "particles": n, "dims": dims}
 
 
+# ------------------------------------------------------------------------------------ batched
+H0 = 1.0 / 64   # cell size of the generated domains (sides are whole numbers of cells)
+
+
+def box_fluid(P, name, dims, rng, ppc):
+    """A domain of dims cells with one seeded fluid box of 10-60% of each axis."""
+    import numpy as np
+    size = np.asarray(dims, dtype=np.float64) * H0
+    ext = rng.uniform(0.1, 0.6, 3)
+    pos = rng.uniform(0.0, 1.0, 3) * (1.0 - ext)
+    lo, hi = pos * size, (pos + ext) * size
+    return P.Fluid(name, [[0.0, 0.0, 0.0], size.tolist()], [P.FluidBlock(lo.tolist(), hi.tolist())],
+                   resolution=int(max(dims)), particles_per_cell=int(ppc), substeps=8)
+
+
+def batched_specs(P, n, seed):
+    """n simulations: each grid side drawn from {32, 48, ..., 192} per axis, one seeded box,
+    4-8 particles per cell (velocities N(0, 0.5) per component via the options)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sides = np.arange(32, 193, 16)
+    return [box_fluid(P, f"b{i}", rng.choice(sides, 3).tolist(), rng, rng.integers(4, 9)) for i in range(n)]
+
+
+def divergence_linf(sim):
+    """max |div v| * dt over fluid cells after the substep's projection (volume change per step)."""
+    import numpy as np
+    nx, ny, nz = sim.dims
+    v = sim.read_grid("vel")
+    nu, nv = (nx + 1) * ny * nz, nx * (ny + 1) * nz
+    u = v[:nu].reshape(nz, ny, nx + 1)
+    w_ = v[nu:nu + nv].reshape(nz, ny + 1, nx)
+    ww = v[nu + nv:].reshape(nz + 1, ny, nx)
+    ct = sim.read_grid("cell_type").reshape(nz, ny, nx)
+    d = (u[:, :, 1:] - u[:, :, :-1]) + (w_[:, 1:, :] - w_[:, :-1, :]) + (ww[1:] - ww[:-1])
+    d = d / sim.cell
+    fl = ct == 1
+    return float(np.max(np.abs(d[fl])) * sim.dt) if fl.any() else 0.0
+
+
+def pct(xs, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else None
+
+
+def run_batched(args, world, rank, local):
+    import numpy as np
+    import pxlengine_gb300 as P
+    n = args.batch_sims
+    fl = batched_specs(P, n, seed=1000 + rank)
+    sims = [P.FluidState(f, fps=15.0, seed=i, options=P.make_options(
+        solver="pcg", rtol=1e-6, max_iter=4000, restart=50, velocity_sigma=0.5, velocity_seed=i + 1))
+        for i, f in enumerate(fl)]
+    N = sum(s.particle_count() for s in sims)
+    cells = sum(int(np.prod(s.dims)) for s in sims)
+    b = P.Batch()
+    for s in sims:
+        b.add(s)
+    tune = b.autotune()
+    b.step(max(0, args.warmup - 1))
+    b.sync()
+    clocks = ClockSampler(local)
+    clocks.start()
+    lat = [b.step_timed(1) for _ in range(args.steps)]
+    clk = clocks.stop()
+    ms = sum(lat)
+    value = N * args.steps * world / (ms / 1e3)
+    div = max(divergence_linf(s) for s in sims[:4])
+    iters = [s.solver_stats()[0] for s in sims]
+    b.close()
+    # the plain per-simulation loop on the same GPU: each simulation advanced alone, one after another
+    for s in sims:
+        s.step(1)
+        s.sync()
+    loop_steps = max(1, min(args.steps, 3))
+    loop_ms = 0.0
+    for _ in range(loop_steps):
+        for s in sims:
+            loop_ms += s.step_timed(1)
+    loop_value = N * loop_steps / (loop_ms / 1e3)
+    for s in sims:
+        s.close()
+    return {"value": value, "ms": ms, "lat": lat, "N": N, "cells": cells, "clk": clk, "tune": tune,
+            "div_linf": div, "iters": iters, "loop_value": loop_value, "loop_ms_per_round": loop_ms / loop_steps}
+
+
+def serve_request(P, rng, i):
+    import numpy as np
+    side = int(np.clip(round(rng.lognormal(np.log(96.0), 0.5)), 32, 256))
+    f = box_fluid(P, f"r{i}", [side, side, side], rng, rng.integers(4, 9))
+    return f, int(rng.integers(50, 501))
+
+
+def run_serve(args, lam, duration, seed):
+    """Poisson arrivals at rate lam for `duration` seconds into a server with a worker thread;
+    then the queue drains. Substep latency = device time of one batched substep."""
+    import numpy as np
+    import pxlengine_gb300 as P
+    from pxlengine_gb300 import _lib as L
+    rng = np.random.default_rng(seed)
+    t, arrivals = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / lam)
+        if t > duration:
+            break
+        arrivals.append(t)
+    reqs = [serve_request(P, rng, i) for i in range(len(arrivals))]
+    opts = P.make_options(solver="pcg", rtol=1e-6, max_iter=4000, restart=50, lift_grid_limits=True,
+                          velocity_sigma=0.5, velocity_seed=7)
+    srv = P.Server(hbm_budget_bytes=150_000_000_000, max_active=256, substeps_per_tick=1, wait_timeout_s=600.0)
+    srv.start()
+    t0 = time.perf_counter()
+    ids = []
+    for ta, (f, nsub) in zip(arrivals, reqs):
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        ids.append(srv.submit(f, nsub, fps=15.0, seed=len(ids), options=opts))
+    deadline = time.perf_counter() + args.serve_drain_s
+    while time.perf_counter() < deadline:
+        st = srv.stats()
+        if st["active"] == 0 and st["queued"] == 0:
+            break
+        time.sleep(0.05)
+    srv.stop()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    done = [srv.status(i) for i in ids]
+    lat = [d.finish_s - d.submit_s for d in done if d.state == L.REQ_DONE]
+    out = {"lambda_per_s": lam, "requests": len(ids), "completed": int(st["completed"]),
+           "rejected": int(st["rejected"]), "particle_substeps_per_s": st["particle_substeps"] / wall,
+           "p50_substep_ms": st["p50_substep_ms"], "p99_substep_ms": st["p99_substep_ms"],
+           "p50_tick_wall_ms": st["p50_tick_wall_ms"], "p99_tick_wall_ms": st["p99_tick_wall_ms"],
+           "p50_request_s": pct(lat, 50), "p99_request_s": pct(lat, 99),
+           "peak_reserved_gb": st["peak_reserved_bytes"] / 1e9, "wall_s": wall,
+           "device_busy_frac": st["busy_device_ms"] / 1e3 / wall}
+    srv.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="dam256", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="dam256", choices=sorted(CONFIGS) + ["batched", "serve"])
+    ap.add_argument("--batch-sims", type=int, default=64)
+    ap.add_argument("--serve-rates", default="2,8")
+    ap.add_argument("--serve-duration-s", type=float, default=15.0)
+    ap.add_argument("--serve-drain-s", type=float, default=120.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     args = ap.parse_args()
-    cfg = CONFIGS[args.config]
+    cfg = CONFIGS.get(args.config)
     rank = env_int("RANK", 0)
     world = env_int("WORLD_SIZE", 1)
     local = env_int("LOCAL_RANK", 0)
     metric = "FLIP particle-substeps/s"
     unit = "particle-substeps/s"
 
+    if args.impl == "reference" and cfg is None:
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no batched or serving form; "
+                              "its CPU arm is timed on the single-simulation configs"}), flush=True)
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -218,6 +368,51 @@ def main():
     lib = L.load()
     if lib.pxf_set_device(local) != 0:
         raise RuntimeError(lib.pxf_last_error(None).decode())
+
+    if args.config == "batched":
+        r = run_batched(args, world, rank, local)
+        if dist:
+            import torch
+            t = torch.tensor([r["ms"]], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            r["value"] = r["N"] * args.steps * world / (float(t.item()) / 1e3)
+        if rank == 0:
+            line = {"metric": metric, "value": r["value"], "unit": unit, "n_gpus": world, "steps": args.steps,
+                    "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                    "data": "synthetic (seeded boxes, reference LCG seeding, N(0,0.5) velocities)",
+                    "config": {"workload": f"batched_{args.batch_sims}_sims", "sims": args.batch_sims,
+                               "particles": r["N"], "cells": r["cells"], "sides": "32..192 per axis",
+                               "pressure": "pcg_fp64dots_rtol1e-6", "parallelism": "replicas",
+                               "l2": "inputs larger than L2"},
+                    "p50_substep_ms": pct(r["lat"], 50), "p99_substep_ms": pct(r["lat"], 99),
+                    "plain_loop": {"value": r["loop_value"], "unit": unit,
+                                   "ms_per_round": r["loop_ms_per_round"],
+                                   "how": "each simulation advanced alone (own graph), one after another"},
+                    "batched_over_loop": r["value"] / world / r["loop_value"], "autotune": r["tune"],
+                    "divergence_linf_dt": r["div_linf"], "pcg_iterations": [min(r["iters"]), max(r["iters"])],
+                    "clocks": r["clk"], "roofline": None, "cpu_baseline": None, "e2e": None}
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
+    if args.config == "serve":
+        rows = [run_serve(args, float(lam), args.serve_duration_s, seed=17 + rank)
+                for lam in args.serve_rates.split(",")]
+        if rank == 0:
+            best = max(rows, key=lambda r: r["particle_substeps_per_s"])
+            line = {"metric": metric, "value": best["particle_substeps_per_s"] * world, "unit": unit,
+                    "n_gpus": world, "steps": None, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f32",
+                    "data": "synthetic (Poisson arrivals, lognormal sides median 96 in [32, 256], seeded boxes)",
+                    "config": {"workload": "serving", "hbm_budget_gb": 150, "substeps": "50..500",
+                               "pressure": "pcg_fp64dots_rtol1e-6", "duration_s": args.serve_duration_s,
+                               "parallelism": "replicas"},
+                    "sweep": rows, "roofline": None, "cpu_baseline": None, "e2e": None}
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     fluid = make_fluid(P, cfg)
     opts = P.make_options(solver=cfg["solver"], rtol=1e-6, max_iter=4000, restart=50,

@@ -176,6 +176,20 @@ typedef struct {
 } pxf_stage_time;
 PXF_API int pxf_profile_substep(pxf_sim* sim, pxf_stage_time* out, uint32_t cap, uint32_t* count);
 
+/* P2G autotuner. No reference counterpart (the reference has one fixed 256-thread dispatch per
+ * kernel, shaders/fluid.slang:93-115). Runs one substep eagerly and, after its counting sort,
+ * times every P2G variant (tile shape x lane mapping) three times on the simulation's own
+ * particles; the fastest of the last two runs is used by every later substep. Every variant
+ * writes the same bits, so the substep's result equals a normal substep's; it counts as one. */
+typedef struct {
+    int32_t tile_shape;   /* 0: 32x8x8, 1: 32x4x4, 2: 16x8x8, 3: 64x4x4, 4: 16x4x4 cells */
+    int32_t lanes;        /* 1: strided lane mapping over a tile's cells, 0: blocked */
+    uint32_t variants;    /* variants timed, in the order shape-major, lanes-minor */
+    float ms[16];         /* device time of each variant, ms */
+    char chosen[32];
+} pxf_tune_result;
+PXF_API int pxf_autotune(pxf_sim* sim, pxf_tune_result* out);
+
 /* Selects the CUDA device of the calling host thread for the simulations it creates (the
  * library links its own CUDA runtime, so a caller's runtime setting does not carry over). */
 PXF_API int pxf_set_device(int device);
@@ -218,6 +232,8 @@ PXF_API void pxf_batch_destroy(pxf_batch* b);
 PXF_API const char* pxf_batch_last_error(const pxf_batch* b);
 /* n substeps of the whole batch with their device time (CUDA events on the batch's stream). */
 PXF_API int pxf_batch_step_timed(pxf_batch* b, uint32_t n_substeps, double* device_ms);
+/* pxf_autotune for the whole batch: one substep of every member, variants timed on all of them. */
+PXF_API int pxf_batch_autotune(pxf_batch* b, pxf_tune_result* out);
 
 /* ------------------------------------------------------------------ serving form
  * A continuous-batching request loop. Requests (a fluid description + a number of substeps) queue

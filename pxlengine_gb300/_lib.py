@@ -42,6 +42,11 @@ class StageTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint32), ("ms", C.c_double)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("tile_shape", C.c_int32), ("lanes", C.c_int32), ("variants", C.c_uint32), ("ms", C.c_float * 16),
+                ("chosen", C.c_char * 32)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active", C.c_uint32), ("substeps_per_tick", C.c_uint32),
                 ("wait_timeout_s", C.c_double)]
@@ -100,6 +105,7 @@ def _sig():
         "pxf_snapshot_free": (None, [vp]),
         "pxf_step_timed": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_double)]),
         "pxf_profile_substep": (C.c_int, [vp, C.POINTER(StageTime), C.c_uint32, u32p]),
+        "pxf_autotune": (C.c_int, [vp, C.POINTER(TuneResult)]),
         "pxf_set_device": (C.c_int, [C.c_int]),
         "pxf_host_alloc": (C.c_int, [C.c_size_t, pp]),
         "pxf_host_free": (None, [vp]),
@@ -115,6 +121,7 @@ def _sig():
         "pxf_batch_destroy": (None, [vp]),
         "pxf_batch_last_error": (C.c_char_p, [vp]),
         "pxf_batch_step_timed": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_double)]),
+        "pxf_batch_autotune": (C.c_int, [vp, C.POINTER(TuneResult)]),
         "pxf_server_config_init": (None, [C.POINTER(ServerConfig)]),
         "pxf_server_create": (C.c_int, [C.POINTER(ServerConfig), pp]),
         "pxf_server_submit": (C.c_int, [vp, dp, C.c_uint32, C.c_double, op, C.c_uint32, C.POINTER(C.c_uint64)]),

@@ -46,6 +46,8 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // --------------------------------------------------------------------------------- batch
 namespace pxf {
 
+struct KernelTimer;
+
 struct BatchImpl {
     std::vector<pxf_sim*> sims;
     cudaStream_t stream = nullptr;
@@ -62,6 +64,16 @@ struct BatchImpl {
     uint32_t max_gs_iters = 0;
     bool any_gs = false, any_pcg = false;
     int tile_shape = 0;
+    int p2g_lanes = 1;                   // 1: strided lane mapping in P2G, 0: blocked
+    bool tuned = false;                  // tile_shape / p2g_lanes chosen by autotune()
+    StageWork w_tiles_s[kMaxP2GShapes];  // P2G tile index of every tile shape
+    uint32_t* d_tile_base = nullptr;
+    size_t cap_tile = 0;
+    uint16_t* d_sim_of = nullptr;        // item -> simulation tables of every stage
+    size_t cap_sim_of = 0;
+    uint32_t* d_act = nullptr;           // compacted item lists of the CG loop's stages
+    uint32_t* d_act_n = nullptr;
+    size_t cap_act = 0;
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
     bool cond_ok = true;                 // conditional while-node usable
@@ -93,6 +105,7 @@ struct BatchImpl {
     int wait();
     void drop_graphs();
     int profile(pxf_stage_time* out, uint32_t cap, uint32_t* count);
+    int run_eager(KernelTimer* timer, pxf_tune_result* tune);
     cudaError_t capture_restart(cudaStream_t st, int n);
 };
 
@@ -228,6 +241,10 @@ BatchImpl::~BatchImpl() {
     if (d_flag) cudaFree(d_flag);
     if (h_flag) cudaFreeHost(h_flag);
     if (d_bar) cudaFree(d_bar);
+    if (d_tile_base) cudaFree(d_tile_base);
+    if (d_sim_of) cudaFree(d_sim_of);
+    if (d_act) cudaFree(d_act);
+    if (d_act_n) cudaFree(d_act_n);
     if (side) cudaStreamDestroy(side);
     if (side2) cudaStreamDestroy(side2);
     if (stream) cudaStreamDestroy(stream);
@@ -257,6 +274,7 @@ int BatchImpl::rebuild() {
     drop_graphs();
     const int n = int(sims.size());
     if (n == 0) { dirty = false; return PXF_OK; }
+    if (n > 65535) return fail(PXF_EINVAL, "a batch holds at most 65535 simulations");
     if (size_t(n) > cap_sims) {
         if (d_sims) cudaFree(d_sims);
         if (d_base) cudaFree(d_base);
@@ -266,11 +284,36 @@ int BatchImpl::rebuild() {
         if ((e = cudaMalloc(&d_sims, cap_sims * sizeof(SimDev))) != cudaSuccess) return cuda_fail(e, "batch table");
         if ((e = cudaMalloc(&d_base, kStages * (cap_sims + 1) * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "batch index");
     }
-    tile_shape = p2g_shape_index();
-    for (pxf_sim* sm : sims)
-        if (sm->opts.p2g_tile >= 0 && sm->opts.p2g_tile < kNumP2GShapes) tile_shape = sm->opts.p2g_tile;
+    if (!tuned) {
+        tile_shape = p2g_shape_index();
+        p2g_lanes = p2g_lanes_default();
+        for (pxf_sim* sm : sims)
+            if (sm->opts.p2g_tile >= 0 && sm->opts.p2g_tile < kNumP2GShapes) tile_shape = sm->opts.p2g_tile;
+    }
     int shape[3];
     p2g_shape(tile_shape, shape);
+    // P2G tile indexes of every shape (the autotuner times them all)
+    if (size_t(n) + 1 > cap_tile) {
+        if (d_tile_base) cudaFree(d_tile_base);
+    if (d_sim_of) cudaFree(d_sim_of);
+    if (d_act) cudaFree(d_act);
+    if (d_act_n) cudaFree(d_act_n);
+        d_tile_base = nullptr;
+        cap_tile = std::max<size_t>(size_t(n) + 1, 2 * cap_tile);
+        if ((e = cudaMalloc(&d_tile_base, kNumP2GShapes * cap_tile * sizeof(uint32_t))) != cudaSuccess)
+            return cuda_fail(e, "tile index");
+    }
+    std::vector<uint32_t> tbase(size_t(kNumP2GShapes) * (n + 1), 0);
+    for (int v = 0; v < kNumP2GShapes; v++) {
+        int sh[3];
+        p2g_shape(v, sh);
+        for (int i = 0; i < n; i++) {
+            const SimDev& d = sims[i]->dev;
+            tbase[v * (n + 1) + i + 1] = tbase[v * (n + 1) + i] + cdiv(d.nx, sh[0]) * cdiv(d.ny, sh[1]) * cdiv(d.nz, sh[2]);
+        }
+    }
+    if ((e = cudaMemcpyAsync(d_tile_base, tbase.data(), tbase.size() * 4, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return cuda_fail(e, "tile index upload");
     std::vector<SimDev> host(n);
     std::vector<uint32_t> base(kStages * (n + 1), 0);
     max_gs_iters = 0;
@@ -334,9 +377,78 @@ int BatchImpl::rebuild() {
         ws[k]->n_sims = n;
         ws[k]->total = base[k * (n + 1) + n];
     }
+    for (int v = 0; v < kNumP2GShapes; v++) {
+        w_tiles_s[v].sims = d_sims;
+        w_tiles_s[v].base = d_tile_base + v * (n + 1);
+        w_tiles_s[v].n_sims = n;
+        w_tiles_s[v].total = tbase[v * (n + 1) + n];
+    }
     pw.sims = d_sims;
     pw.n_sims = n;
     pw.chunks = w_chunks;
+    pw.chunks_all = w_chunks;
+    // simulation of every item of every stage (one load instead of a search), for several simulations
+    {
+        size_t total = 0;
+        std::vector<StageWork*> all(ws, ws + kStages);
+        for (int v = 0; v < kNumP2GShapes; v++) all.push_back(&w_tiles_s[v]);
+        for (StageWork* w : all) total += w->total;
+        std::vector<uint16_t> sim_of;
+        if (n > 1) {
+            sim_of.resize(total);
+            size_t off = 0;
+            for (StageWork* w : all) {
+                const uint32_t* b = (w >= &w_tiles_s[0] && w < &w_tiles_s[0] + kMaxP2GShapes)
+                                        ? tbase.data() + (w - &w_tiles_s[0]) * (n + 1)
+                                        : base.data() + (std::find(ws, ws + kStages, w) - ws) * (n + 1);
+                for (int i = 0; i < n; i++)
+                    for (uint32_t it = b[i]; it < b[i + 1]; it++) sim_of[off + it] = uint16_t(i);
+                off += w->total;
+            }
+        }
+        if (sim_of.size() > cap_sim_of) {
+            if (d_sim_of) cudaFree(d_sim_of);
+            d_sim_of = nullptr;
+            cap_sim_of = std::max(sim_of.size(), 2 * cap_sim_of);
+            if ((e = cudaMalloc(&d_sim_of, cap_sim_of * sizeof(uint16_t))) != cudaSuccess) return cuda_fail(e, "item table");
+        }
+        if (!sim_of.empty() &&
+            (e = cudaMemcpyAsync(d_sim_of, sim_of.data(), sim_of.size() * 2, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+            return cuda_fail(e, "item table upload");
+        size_t off = 0;
+        for (StageWork* w : all) {
+            w->sim_of = n > 1 ? d_sim_of + off : nullptr;
+            off += w->total;
+        }
+        pw.chunks.sim_of = pw.chunks_all.sim_of = w_chunks.sim_of;
+        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "item table upload");
+    }
+    // compacted item lists of the CG loop's stages
+    if (any_pcg) {
+        size_t need = pw.chunks.total;
+        for (int l = 0; l < kMaxLevels; l++) need += pw.level[l].total + pw.coarse[l].total;
+        if (need > cap_act) {
+            if (d_act) cudaFree(d_act);
+            d_act = nullptr;
+            cap_act = std::max(need, 2 * cap_act);
+            if ((e = cudaMalloc(&d_act, cap_act * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "work lists");
+        }
+        if (!d_act_n && (e = cudaMalloc(&d_act_n, kActCounters * sizeof(uint32_t))) != cudaSuccess)
+            return cuda_fail(e, "work lists");
+        size_t off = 0;
+        pw.act_n = d_act_n;
+        pw.chunks.act = d_act + off;
+        pw.chunks.act_n = d_act_n;
+        off += pw.chunks.total;
+        for (int l = 0; l < kMaxLevels; l++) {
+            pw.level[l].act = d_act + off;
+            pw.level[l].act_n = d_act_n + 1 + l;
+            off += pw.level[l].total;
+            pw.coarse[l].act = d_act + off;
+            pw.coarse[l].act_n = d_act_n + 1 + kMaxLevels + l;
+            off += pw.coarse[l].total;
+        }
+    }
     if (pw.any_mg && (e = mg_tail_attr(pw.tail_smem)) != cudaSuccess) return cuda_fail(e, "tail kernel attribute");
     if (any_pcg && !d_bar) {
         if ((e = cudaMalloc(&d_bar, sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
@@ -354,7 +466,7 @@ int BatchImpl::record_gs_part(cudaStream_t st) {
     cudaError_t e;
     if ((e = launch_scan(w_chunks, d_sims, n, st)) != cudaSuccess) return cuda_fail(e, "scan");
     if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
-    if ((e = launch_p2g(w_tiles, tile_shape, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+    if ((e = launch_p2g(w_tiles, tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
     if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
     if (any_gs) {
         for (uint32_t it = 0; it < max_gs_iters; it++)
@@ -376,7 +488,7 @@ int BatchImpl::record_pre(cudaStream_t st) {
     cudaError_t e;
     if ((e = launch_scan(w_chunks, d_sims, n, st)) != cudaSuccess) return cuda_fail(e, "scan");
     if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
-    if ((e = launch_p2g(w_tiles, tile_shape, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+    if ((e = launch_p2g(w_tiles, tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
     if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
     if (any_gs) {
         for (uint32_t it = 0; it < max_gs_iters; it++)
@@ -617,8 +729,8 @@ int BatchImpl::step(uint32_t nsteps) {
 struct KernelTimer : LaunchLog {
     cudaStream_t stream;
     std::vector<cudaEvent_t> evs;
-    std::vector<std::pair<size_t, const char*>> spans;   // (index of the event ending the kernel, name)
-    size_t prev = 0;
+    std::vector<std::pair<size_t, const char*>> spans;     // (index of the event ending the kernel, name)
+    std::vector<std::pair<size_t, size_t>> segments;       // (first span of a segment, its start event)
     bool ok = true;
     explicit KernelTimer(cudaStream_t s) : stream(s) {}
     ~KernelTimer() {
@@ -633,89 +745,135 @@ struct KernelTimer : LaunchLog {
     // Starts a segment: a hold kernel long enough for the host to queue the segment behind it.
     void segment(double hold_us) {
         launch_hold((long long)(hold_us * 2.1e3), stream);
-        prev = record();
+        segments.push_back({spans.size(), record()});
     }
     void launched(const char* kernel, cudaStream_t st) override {
         if (st != stream) return;
         const size_t e = record();
         spans.push_back({e, kernel});
     }
+    // Event that starts span i: the segment start for a segment's first kernel, else the end of
+    // the kernel before it.
+    size_t start_of(size_t i) const {
+        size_t from = 0;
+        for (const auto& sg : segments)
+            if (sg.first <= i) from = sg.first == i ? sg.second : spans[i - 1].first;
+        return from;
+    }
 };
 
-// One substep launched kernel by kernel (eager, no graph) with an event after each kernel.
-// Records are per kernel name, in order of first launch: launches and summed device time.
-int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
+// One substep launched eagerly (no graph). With a timer: a hold kernel starts each segment the
+// host queues in one go. With `tune`: after the counting sort every P2G variant (tile shape x
+// lane mapping) runs three times with events around it; the fastest of the last two runs becomes
+// the batch's choice. Every variant writes the same bits, so the substep's result is unchanged.
+int BatchImpl::run_eager(KernelTimer* timer, pxf_tune_result* tune) {
     if (dirty) {
         int rc = rebuild();
         if (rc) return rc;
     }
     const int n = int(sims.size());
+    cudaError_t e;
+    if (timer) timer->segment(1000.0 + 40.0 * (any_gs ? max_gs_iters : 0));
+    if ((e = launch_scan(w_chunks, d_sims, n, stream)) != cudaSuccess) return cuda_fail(e, "scan");
+    if ((e = launch_scatter(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "scatter");
+    if (tune) {
+        const int nv = kNumP2GShapes * 2;
+        std::vector<cudaEvent_t> evs(2 * nv * 3, nullptr);
+        for (auto& x : evs)
+            if ((e = cudaEventCreate(&x)) != cudaSuccess) return cuda_fail(e, "tune events");
+        for (int rep = 0; rep < 3; rep++)
+            for (int v = 0; v < nv; v++) {
+                const int shape = v >> 1, lanes = v & 1;
+                cudaEventRecord(evs[2 * (rep * nv + v)], stream);
+                if ((e = launch_p2g(w_tiles_s[shape], shape, lanes, stream)) != cudaSuccess) return cuda_fail(e, "p2g");
+                cudaEventRecord(evs[2 * (rep * nv + v) + 1], stream);
+            }
+        int rc = wait();
+        if (rc) return rc;
+        int best = 0;
+        float best_ms = 0;
+        std::memset(tune, 0, sizeof(*tune));
+        tune->variants = uint32_t(nv);
+        for (int v = 0; v < nv; v++) {
+            float m = 1e30f;
+            for (int rep = 1; rep < 3; rep++) {
+                float t = 0;
+                cudaEventElapsedTime(&t, evs[2 * (rep * nv + v)], evs[2 * (rep * nv + v) + 1]);
+                m = std::min(m, t);
+            }
+            if (v < 16) tune->ms[v] = m;
+            if (v == 0 || m < best_ms) { best = v; best_ms = m; }
+        }
+        for (auto& x : evs) cudaEventDestroy(x);
+        tile_shape = best >> 1;
+        p2g_lanes = best & 1;
+        tuned = true;
+        w_tiles = w_tiles_s[tile_shape];
+        tune->tile_shape = tile_shape;
+        tune->lanes = p2g_lanes;
+        int sh[3];
+        p2g_shape(tile_shape, sh);
+        std::snprintf(tune->chosen, sizeof(tune->chosen), "p2g %dx%dx%d %s", sh[0], sh[1], sh[2],
+                      p2g_lanes ? "strided" : "blocked");
+        dirty = true;    // recapture: later substeps use the chosen variant
+    } else if ((e = launch_p2g(w_tiles, tile_shape, p2g_lanes, stream)) != cudaSuccess) {
+        return cuda_fail(e, "p2g");
+    }
+    if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
+    if (any_gs) {
+        for (uint32_t it = 0; it < max_gs_iters; it++)
+            for (uint32_t parity = 0; parity < 2; parity++)
+                if ((e = launch_pressure_rb(w_half, parity, it, stream)) != cudaSuccess) return cuda_fail(e, "pressure");
+    }
+    if (any_pcg && persistent) {
+        if ((e = launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream)) != cudaSuccess)
+            return cuda_fail(e, "pcg solve");
+    } else if (any_pcg) {
+        if (!d_flag) {
+            if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+            if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
+        }
+        if ((e = launch_pcg_init(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
+        for (uint32_t guard = 0; guard < 100000; guard++) {
+            if ((e = launch_pcg_any(d_sims, n, d_flag, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+            cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
+            int rc = wait();
+            if (rc) return rc;
+            if (*h_flag == 0) break;
+            if (timer) timer->segment(1000.0);
+            if ((e = launch_pcg_body(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
+        }
+        if (timer) timer->segment(200.0);
+        if ((e = launch_pcg_finish(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
+    }
+    if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
+    if ((e = launch_g2p(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "g2p");
+    int rc = wait();
+    if (rc) return rc;
+    for (pxf_sim* sm : sims) sm->steps_done += 1;
+    return PXF_OK;
+}
+
+// One substep launched kernel by kernel (eager, no graph) with an event after each kernel.
+// Records are per kernel name, in order of first launch: launches and summed device time.
+int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
     KernelTimer timer(stream);
-    std::vector<size_t> seg_start;   // span index -> event index that precedes it
     struct Guard {
         LaunchLog* old;
         explicit Guard(LaunchLog* l) : old(g_launch_log) { g_launch_log = l; }
         ~Guard() { g_launch_log = old; }
     };
-    cudaError_t e;
     {
         Guard g(&timer);
-        // pre-solve kernels (and the whole red-black schedule) in one segment
-        timer.segment(1000.0 + 40.0 * (any_gs ? max_gs_iters : 0));
-        std::vector<std::pair<size_t, size_t>> starts;   // (first span of the segment, its start event)
-        auto mark_segment = [&]() { starts.push_back({timer.spans.size(), timer.prev}); };
-        mark_segment();
-        if ((e = launch_scan(w_chunks, d_sims, n, stream)) != cudaSuccess) return cuda_fail(e, "scan");
-        if ((e = launch_scatter(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "scatter");
-        if ((e = launch_p2g(w_tiles, tile_shape, stream)) != cudaSuccess) return cuda_fail(e, "p2g");
-        if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
-        if (any_gs) {
-            for (uint32_t it = 0; it < max_gs_iters; it++)
-                for (uint32_t parity = 0; parity < 2; parity++)
-                    if ((e = launch_pressure_rb(w_half, parity, it, stream)) != cudaSuccess)
-                        return cuda_fail(e, "pressure");
-        }
-        if (any_pcg && persistent) {
-            if ((e = launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream)) != cudaSuccess)
-                return cuda_fail(e, "pcg solve");
-        } else if (any_pcg) {
-            if (!d_flag) {
-                if ((e = cudaMalloc(&d_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
-                if ((e = cudaMallocHost(&h_flag, 4)) != cudaSuccess) return cuda_fail(e, "flag");
-            }
-            if ((e = launch_pcg_init(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg init");
-            for (uint32_t guard = 0; guard < 100000; guard++) {
-                if ((e = launch_pcg_any(d_sims, n, d_flag, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-                cudaMemcpyAsync(h_flag, d_flag, 4, cudaMemcpyDeviceToHost, stream);
-                int rc = wait();
-                if (rc) return rc;
-                if (*h_flag == 0) break;
-                timer.segment(1000.0);
-                mark_segment();
-                if ((e = launch_pcg_body(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg");
-            }
-            timer.segment(200.0);
-            mark_segment();
-            if ((e = launch_pcg_finish(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
-        }
-        if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
-        if ((e = launch_g2p(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "g2p");
-        int rc = wait();
+        int rc = run_eager(&timer, nullptr);
         if (rc) return rc;
-        if (!timer.ok) return fail(PXF_ECUDA, "profiler events");
-        // each span starts at the event before it (the segment start for a segment's first kernel)
-        size_t si = 0;
-        for (size_t i = 0; i < timer.spans.size(); i++) {
-            while (si + 1 < starts.size() && starts[si + 1].first <= i) si++;
-            const size_t from = (i == starts[si].first) ? starts[si].second : timer.spans[i - 1].first;
-            seg_start.push_back(from);
-        }
     }
+    if (!timer.ok) return fail(PXF_ECUDA, "profiler events");
     struct Rec { const char* name; uint32_t launches; double ms; };
     std::vector<Rec> recs;
     for (size_t i = 0; i < timer.spans.size(); i++) {
         float ms = 0;
-        cudaEventElapsedTime(&ms, timer.evs[seg_start[i]], timer.evs[timer.spans[i].first]);
+        cudaEventElapsedTime(&ms, timer.evs[timer.start_of(i)], timer.evs[timer.spans[i].first]);
         const char* name = timer.spans[i].second;
         int k = -1;
         for (size_t j = 0; j < recs.size(); j++) if (std::strcmp(recs[j].name, name) == 0) k = int(j);
@@ -723,7 +881,6 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
         recs[k].launches++;
         recs[k].ms += ms;
     }
-    for (pxf_sim* s : sims) s->steps_done += 1;
     *count = uint32_t(recs.size());
     for (uint32_t i = 0; i < cap && i < recs.size(); i++) {
         std::snprintf(out[i].name, sizeof(out[i].name), "%s", recs[i].name);
@@ -734,6 +891,11 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
 }
 
 void set_global_error_message(const std::string& m) { g_last_error = m; }
+
+int p2g_lanes_default() {
+    static const int lanes = [] { const char* v = std::getenv("PXF_P2G_STRIDED"); return v ? (std::atoi(v) ? 1 : 0) : 1; }();
+    return lanes;
+}
 
 int p2g_shape_index() {
     static int shape = -2;
@@ -1399,6 +1561,23 @@ void pxf_batch_destroy(pxf_batch* b) {
 }
 
 const char* pxf_batch_last_error(const pxf_batch* b) { return b ? b->impl.err.c_str() : g_last_error.c_str(); }
+
+int pxf_autotune(pxf_sim* s, pxf_tune_result* out) {
+    if (!s || !out) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (s->batch && s->batch != s->own) return s->fail(PXF_ESTATE, "simulation is stepped by a batch");
+    s->initialized = true;
+    int rc = s->own->run_eager(nullptr, out);
+    if (rc) return s->fail(rc, s->own->err);
+    return PXF_OK;
+}
+
+int pxf_batch_autotune(pxf_batch* b, pxf_tune_result* out) {
+    if (!b || !out) return set_global_error(PXF_EINVAL, "NULL argument");
+    BatchImpl& B = b->impl;
+    if (B.sims.empty()) return B.fail(PXF_ESTATE, "empty batch");
+    for (pxf_sim* s : B.sims) s->initialized = true;
+    return B.run_eager(nullptr, out);
+}
 
 int pxf_batch_step_timed(pxf_batch* b, uint32_t n, double* ms) {
     if (!b || !ms) return set_global_error(PXF_EINVAL, "NULL argument");

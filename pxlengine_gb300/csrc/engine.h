@@ -5,5 +5,6 @@ namespace pxf {
 
 // Default P2G tile shape index (PXF_P2G_TILE environment variable, else 0).
 int p2g_shape_index();
+int p2g_lanes_default();
 
 }  // namespace pxf

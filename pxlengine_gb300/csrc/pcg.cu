@@ -156,7 +156,8 @@ __device__ __forceinline__ void dep_wait() {
 // Compacts each chunk of level l into its red then black system cells, in ascending cell order.
 __device__ void ph_cell_lists(const Work& w, int l) {
     __shared__ uint32_t wr[32], wb[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1) continue;
@@ -202,9 +203,44 @@ __device__ void ph_cell_lists(const Work& w, int l) {
     }
 }
 
+// Appends the items of stage w whose chunk of level `lev` holds system cells to the stage's act
+// list (one thread per item; the order of the list does not matter: items are independent and
+// every reduction keeps one partial per chunk). With zero_partial, empty level-0 chunks get a
+// zero partial, which no later step overwrites.
+__device__ void compact_stage(const Work& w, int lev, uint32_t* count, bool zero_partial) {
+    uint32_t* out = const_cast<uint32_t*>(w.act);
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < w.total; item += gridDim.x * blockDim.x) {
+        const int si = find_sim(w, item);
+        const SimDev* sp = w.sims + si;
+        if (sp->solver != 1) continue;
+        const uint32_t chunk = item - __ldg(w.base + si);
+        const MgLevel& L = sp->lev[lev];
+        const uint32_t n = __ldcg(L.lcnt + 2 * chunk) + __ldcg(L.lcnt + 2 * chunk + 1);
+        if (n) out[atomicAdd(count, 1u)] = item;
+        else if (zero_partial) sp->partial[chunk] = 0.0;
+    }
+}
+
+__device__ void ph_compact(const PcgWork& pw) {
+    Work c = pw.chunks_all;
+    c.act = pw.chunks.act;
+    compact_stage(c, 0, pw.act_n, true);
+    for (int l = 0; l + 1 < pw.max_levels; l++) {
+        if (pw.level[l].total) {
+            Work a = pw.level[l];
+            compact_stage(a, l, pw.act_n + 1 + l, false);
+        }
+        if (pw.coarse[l].total) {
+            Work b = pw.coarse[l];
+            compact_stage(b, l + 1, pw.act_n + 1 + kMaxLevelsK + l, false);
+        }
+    }
+}
+
 // Type of level l+1 from its children on level l (work: level-(l+1) chunks).
 __device__ void ph_coarsen(const Work& w, int l) {
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1) continue;
@@ -231,7 +267,8 @@ __device__ void ph_coarsen(const Work& w, int l) {
 
 // Neighbour record of level l+1 (as k_divergence builds it for level 0).
 __device__ void ph_info(const Work& w, int l) {
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1) continue;
@@ -269,7 +306,8 @@ __device__ void ph_info(const Work& w, int l) {
 // (fused prolongation); mode 3: as 0, then the chunk's partial r.z over all system cells.
 __device__ void ph_smooth(const Work& w, int l, int color, int mode) {
     __shared__ double sh[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1 || sp->precond != 0) continue;
@@ -331,7 +369,8 @@ __device__ void ph_smooth(const Work& w, int l, int color, int mode) {
 // r_{l+1} = 1/2 * sum over the children of their residual r - A z (level l); 8 lanes per coarse
 // cell, children summed by a fixed shuffle tree. Work: level-(l+1) chunks.
 __device__ void ph_restrict(const Work& w, int l) {
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
         if (sp->solver != 1 || sp->precond != 0) continue;
@@ -557,7 +596,8 @@ __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
 // Jacobi preconditioner: z = r / cnt, partial r.z.
 __device__ void ph_jacobi(const Work& w) {
     __shared__ double sh[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1 || s.precond != 1) continue;
@@ -584,7 +624,8 @@ __device__ void ph_jacobi(const Work& w) {
 // Partial |b|^2.
 __device__ void ph_init(const Work& w) {
     __shared__ double sh[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
@@ -604,7 +645,8 @@ __device__ void ph_init(const Work& w) {
 
 // x64 = hi + lo for simulations about to restart (or x = 0 for a zero right-hand side).
 __device__ void ph_widen(const Work& w) {
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
@@ -631,7 +673,8 @@ __device__ void ph_widen(const Work& w) {
 // FP64 restart residual r = b - A x and its partial |r|^2.
 __device__ void ph_resid(const Work& w) {
     __shared__ double sh[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
@@ -675,7 +718,8 @@ __device__ void ph_resid(const Work& w) {
 // partial p'.Ap.
 __device__ void ph_dir(const Work& w) {
     __shared__ double sh[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
@@ -721,7 +765,8 @@ __device__ void ph_dir(const Work& w) {
 // x += alpha p (double-float), r -= alpha Ap (FP32), partial |r|^2.
 __device__ void ph_update(const Work& w) {
     __shared__ double sh[32];
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
@@ -763,7 +808,8 @@ __device__ void ph_update(const Work& w) {
 
 // FP32 pressure copy and the FP64 solution at the end of the solve (all cells).
 __device__ void ph_finish(const Work& w) {
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
@@ -882,6 +928,7 @@ __global__ void __launch_bounds__(1024, 1) k_mg_tail(const SimDev* sims, int n_s
     ph_tail(sims, n_sims, tsm);
     dep_wait();
 }
+__global__ void __launch_bounds__(THREADS) k_compact(PcgWork pw) { ph_compact(pw); }
 __global__ void __launch_bounds__(THREADS) k_jacobi(Work w) { ph_jacobi(w); dep_wait(); }
 __global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) { ph_init(w); }
 __global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) { ph_widen(w); dep_wait(); }
@@ -985,7 +1032,7 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
     extern __shared__ float tsm[];
     const PcgWork& pw = a.pw;
     // multigrid setup: system-cell lists and the coarse levels
-    ph_cell_lists(pw.chunks, 0);
+    ph_cell_lists(pw.chunks_all, 0);
     SYNC_OR_RETURN();
     for (int l = 0; l + 1 < pw.setup_levels; l++) {
         if (!pw.setup[l].total) continue;
@@ -996,6 +1043,8 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
         ph_cell_lists(pw.setup[l], l + 1);
         SYNC_OR_RETURN();
     }
+    ph_compact(pw);
+    SYNC_OR_RETURN();
     ph_init(pw.chunks);
     SYNC_OR_RETURN();
     ph_ctl(pw.sims, pw.n_sims, 0);
@@ -1015,7 +1064,7 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
         if (any_restart(pw.sims, pw.n_sims) && !solve_restart(a)) return;
         if (!solve_precond(a, tsm)) return;
     }
-    ph_finish(pw.chunks);
+    ph_finish(pw.chunks_all);
 }
 
 // ============================================================================ launchers
@@ -1023,13 +1072,14 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
 // the rest to whichever SM frees first.
 static unsigned grid_of(uint32_t total) { return total ? total : 1u; }
 
-static inline Work mkw(const StageWork& sw) {
-    Work w;
-    w.sims = sw.sims;
-    w.base = sw.base;
-    w.n_sims = sw.n_sims;
-    w.total = sw.total;
-    return w;
+static inline Work mkw(const StageWork& sw) { return sw; }
+
+// Grid of a stage: one block per item for a full stage; for a compacted stage (its length is
+// known only on the device) at most 8 blocks per SM, block-strided over the list.
+static unsigned grid_w(const StageWork& w) {
+    if (!w.act) return grid_of(w.total);
+    const uint32_t cap = uint32_t(sm_count()) * 8u;
+    return w.total < cap ? (w.total ? w.total : 1u) : cap;
 }
 
 // Launch of a CG-loop kernel with programmatic stream serialization (it may start while the
@@ -1064,58 +1114,62 @@ cudaError_t mg_tail_attr(size_t smem) {
 }
 
 cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
-    k_cell_lists<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks), 0); note_launch("k_cell_lists", st);
+    k_cell_lists<<<grid_of(pw.chunks_all.total), THREADS, 0, st>>>(mkw(pw.chunks_all), 0); note_launch("k_cell_lists", st);
     for (int l = 0; l + 1 < pw.setup_levels; l++) {
         if (!pw.setup[l].total) continue;
         k_mg_coarsen<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l); note_launch("k_mg_coarsen", st);
         k_mg_info<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l); note_launch("k_mg_info", st);
         k_cell_lists<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l + 1); note_launch("k_cell_lists", st);
     }
+    cudaError_t e = cudaMemsetAsync(pw.act_n, 0, kActCounters * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const unsigned gc = std::min<unsigned>((pw.chunks_all.total + THREADS - 1) / THREADS, unsigned(sm_count()) * 4u);
+    k_compact<<<gc ? gc : 1u, THREADS, 0, st>>>(pw); note_launch("k_compact", st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
     if (pw.any_jacobi) {
-        launch_dep("k_jacobi", k_jacobi, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
+        launch_dep("k_jacobi", k_jacobi, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     }
     if (pw.any_mg) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
             // (the red half sweep from zero ran in the kernel that produced this level's r)
-            launch_dep("k_mg_smooth", k_mg_smooth, grid_of(pw.level[l].total), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0);
-            launch_dep("k_mg_restrict", k_mg_restrict, grid_of(pw.coarse[l].total), THREADS, 0, st, mkw(pw.coarse[l]), l);
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0);
+            launch_dep("k_mg_restrict", k_mg_restrict, grid_w(pw.coarse[l]), THREADS, 0, st, mkw(pw.coarse[l]), l);
         }
         launch_dep("k_mg_tail", k_mg_tail, pw.n_sims, 1024, pw.tail_smem, st, pw.sims, pw.n_sims);
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
-            launch_dep("k_mg_smooth", k_mg_smooth, grid_of(pw.level[l].total), THREADS, 0, st, mkw(pw.level[l]), l, 1, 2);
-            launch_dep("k_mg_smooth", k_mg_smooth, grid_of(pw.level[l].total), THREADS, 0, st, mkw(pw.level[l]), l, 0, l == 0 ? 3 : 0);
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 2);
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 0, l == 0 ? 3 : 0);
         }
     }
     return ctl(pw, 2, st);
 }
 
 cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st) {
-    launch_dep("k_pcg_widen", k_pcg_widen, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
-    launch_dep("k_pcg_resid", k_pcg_resid, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
+    launch_dep("k_pcg_widen", k_pcg_widen, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
+    launch_dep("k_pcg_resid", k_pcg_resid, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     return ctl(pw, 1, st);
 }
 
 cudaError_t launch_pcg_init(const PcgWork& pw, cudaStream_t st) {
     launch_mg_setup(pw, st);
-    k_pcg_init<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks)); note_launch("k_pcg_init", st);
+    k_pcg_init<<<grid_w(pw.chunks), THREADS, 0, st>>>(mkw(pw.chunks)); note_launch("k_pcg_init", st);
     ctl(pw, 0, st);
     launch_pcg_restart(pw, st);
     return launch_precond(pw, st);
 }
 
 cudaError_t launch_pcg_dir(const PcgWork& pw, cudaStream_t st) {
-    launch_dep("k_pcg_dir", k_pcg_dir, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
+    launch_dep("k_pcg_dir", k_pcg_dir, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     return ctl(pw, 3, st);
 }
 
 cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st) {
-    launch_dep("k_pcg_update", k_pcg_update, grid_of(pw.chunks.total), THREADS, 0, st, mkw(pw.chunks));
+    launch_dep("k_pcg_update", k_pcg_update, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     return ctl(pw, 4, st);
 }
 
@@ -1142,7 +1196,7 @@ cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaS
 }
 
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st) {
-    k_pcg_finish<<<grid_of(pw.chunks.total), THREADS, 0, st>>>(mkw(pw.chunks)); note_launch("k_pcg_finish", st);
+    k_pcg_finish<<<grid_of(pw.chunks_all.total), THREADS, 0, st>>>(mkw(pw.chunks_all)); note_launch("k_pcg_finish", st);
     return cudaGetLastError();
 }
 
@@ -1157,6 +1211,7 @@ int pcg_solve_grid(size_t smem) {
 cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(pw.act_n, 0, kActCounters * sizeof(uint32_t), st)) != cudaSuccess) return e;
     SolveArgs a;
     a.pw = pw;
     a.bar = bar;

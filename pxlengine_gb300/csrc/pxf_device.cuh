@@ -90,12 +90,16 @@ struct SimDev {
 // base[s] <= i < base[s + 1].
 struct Work {
     const SimDev* sims = nullptr;
-    const uint32_t* base = nullptr;   // n_sims + 1 entries, device memory
+    const uint32_t* base = nullptr;     // n_sims + 1 entries, device memory
     int n_sims = 0;
     uint32_t total = 0;
+    const uint16_t* sim_of = nullptr;   // simulation of every item (batches of several simulations)
+    const uint32_t* act = nullptr;      // the items that have work, built on the device; null: all
+    const uint32_t* act_n = nullptr;    // number of entries of act
 };
 
 __device__ __forceinline__ int find_sim(const Work& w, uint32_t item) {
+    if (w.sim_of) return __ldg(w.sim_of + item);
     int lo = 0, hi = w.n_sims;
     while (hi - lo > 1) {
         int mid = (lo + hi) >> 1;
@@ -103,6 +107,10 @@ __device__ __forceinline__ int find_sim(const Work& w, uint32_t item) {
     }
     return lo;
 }
+
+// Items a block-strided loop visits: the compacted list when there is one, else every item.
+__device__ __forceinline__ uint32_t work_count(const Work& w) { return w.act ? __ldcg(w.act_n) : w.total; }
+__device__ __forceinline__ uint32_t work_item(const Work& w, uint32_t k) { return w.act ? __ldcg(w.act + k) : k; }
 
 // float -> int32, truncating (cvt.rzi.s32.f32: NaN -> 0, saturating).
 __device__ __forceinline__ int f2i(float x) { return __float2int_rz(x); }

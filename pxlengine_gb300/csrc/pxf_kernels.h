@@ -34,11 +34,13 @@ cudaError_t launch_hold(long long cycles, cudaStream_t st);
 int grid_cap_per_sm();
 void p2g_shape(int shape, int out[3]);
 extern const int kNumP2GShapes;
+constexpr int kMaxP2GShapes = 8;   // capacity of per-shape tables (kNumP2GShapes <= this)
 
 cudaError_t launch_scan(const StageWork& chunks, const SimDev* sims, int n_sims, cudaStream_t st);
 cudaError_t launch_scatter(const StageWork& parts, cudaStream_t st);
 cudaError_t launch_bin(const StageWork& parts, cudaStream_t st);
-cudaError_t launch_p2g(const StageWork& tiles, int shape, cudaStream_t st);
+// lanes: 1 = strided lane mapping over a tile's cells, 0 = blocked.
+cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, cudaStream_t st);
 cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st);
 cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st);
 cudaError_t launch_project(const StageWork& faces, cudaStream_t st);
@@ -49,13 +51,17 @@ cudaError_t launch_scatter_aos(const SimDev& s, const float4* in, cudaStream_t s
 cudaError_t launch_counts_from_start(const SimDev& s, uint32_t* out, cudaStream_t st);
 
 // Work indexes of the precision solver for one batch.
+// The CG loop's stages visit only chunks that hold system cells: after the cell lists are built,
+// one kernel compacts each stage's items into act[] / act_n (counters zeroed before it).
 struct PcgWork {
     const SimDev* sims = nullptr;
     int n_sims = 0;
-    StageWork chunks;                 // level-0 chunks of kScanChunk cells (precision simulations)
-    StageWork level[kMaxLevelsK];     // level-l chunks of multigrid simulations with a level below l
-    StageWork coarse[kMaxLevelsK];    // level-(l+1) chunks of those simulations
+    StageWork chunks;                 // level-0 chunks of kScanChunk cells (precision simulations), compacted
+    StageWork chunks_all;             // the same items, every chunk (list building, final copy)
+    StageWork level[kMaxLevelsK];     // level-l chunks of multigrid simulations with a level below l, compacted
+    StageWork coarse[kMaxLevelsK];    // level-(l+1) chunks of those simulations, compacted
     StageWork setup[kMaxLevelsK];     // level-(l+1) chunks of every multigrid simulation with level l+1
+    uint32_t* act_n = nullptr;        // counters: [0] chunks, [1 + l] level[l], [1 + kMaxLevelsK + l] coarse[l]
     int setup_levels = 0;
     int max_levels = 0;                 // global-memory levels (below the shared-memory tail)
     bool any_mg = false, any_jacobi = false;
@@ -80,6 +86,7 @@ constexpr long long kBarrierCycles = 4000000000LL;   // about 2 s at the GB300's
 
 // One cooperative launch that runs the whole precision solve of a substep.
 int pcg_solve_grid(size_t smem);
+constexpr int kActCounters = 1 + 2 * kMaxLevelsK;
 cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st);
 
 // Precision solver: multigrid setup + |b|^2 + state reset + first restart + first z = M^-1 r;

@@ -679,7 +679,7 @@ static inline Work mk(const StageWork& sw) {
 }
 
 template <int TX, int TY, int TZ>
-static cudaError_t launch_p2g_t(const StageWork& sw, cudaStream_t st) {
+static cudaError_t launch_p2g_t(const StageWork& sw, int lanes, cudaStream_t st) {
     using T = P2GTile<TX, TY, TZ>;
     static bool attr = false;
     if (!attr) {
@@ -690,17 +690,17 @@ static cudaError_t launch_p2g_t(const StageWork& sw, cudaStream_t st) {
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_p2g<TX, TY, TZ>, 256, T::SMEM);
     if (per_sm < 1) per_sm = 1;
-    static const int strided = [] { const char* v = std::getenv("PXF_P2G_STRIDED"); return v ? std::atoi(v) : 1; }();
     static const int pack = [] { const char* v = std::getenv("PXF_P2G_PACKED"); return v ? std::atoi(v) : 0; }();
     // One block per tile: tiles of the liquid hold most of the work and those of the air none, so
     // the block scheduler's dynamic assignment balances the SMs (a grid-strided loop would not).
     (void)per_sm;
-    k_p2g<TX, TY, TZ><<<sw.total ? sw.total : 1u, 256, T::SMEM, st>>>(mk(sw), strided, pack); note_launch("k_p2g", st);
+    k_p2g<TX, TY, TZ><<<sw.total ? sw.total : 1u, 256, T::SMEM, st>>>(mk(sw), lanes, pack); note_launch("k_p2g", st);
     return cudaGetLastError();
 }
 
 const int kP2GShapes[][3] = {{32, 8, 8}, {32, 4, 4}, {16, 8, 8}, {64, 4, 4}, {16, 4, 4}};
 const int kNumP2GShapes = 5;
+static_assert(5 <= kMaxP2GShapes, "per-shape tables");
 
 void p2g_shape(int shape, int out[3]) {
     if (shape < 0 || shape >= kNumP2GShapes) shape = 0;
@@ -709,13 +709,13 @@ void p2g_shape(int shape, int out[3]) {
     out[2] = kP2GShapes[shape][2];
 }
 
-cudaError_t launch_p2g(const StageWork& sw, int shape, cudaStream_t st) {
+cudaError_t launch_p2g(const StageWork& sw, int shape, int lanes, cudaStream_t st) {
     switch (shape) {
-        case 1: return launch_p2g_t<32, 4, 4>(sw, st);
-        case 2: return launch_p2g_t<16, 8, 8>(sw, st);
-        case 3: return launch_p2g_t<64, 4, 4>(sw, st);
-        case 4: return launch_p2g_t<16, 4, 4>(sw, st);
-        default: return launch_p2g_t<32, 8, 8>(sw, st);
+        case 1: return launch_p2g_t<32, 4, 4>(sw, lanes, st);
+        case 2: return launch_p2g_t<16, 8, 8>(sw, lanes, st);
+        case 3: return launch_p2g_t<64, 4, 4>(sw, lanes, st);
+        case 4: return launch_p2g_t<16, 4, 4>(sw, lanes, st);
+        default: return launch_p2g_t<32, 8, 8>(sw, lanes, st);
     }
 }
 

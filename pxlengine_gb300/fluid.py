@@ -215,6 +215,12 @@ class FluidState:
         _check(self._lib.pxf_profile_substep(self.h, recs, 32, C.byref(cnt)), self.h)
         return [(recs[i].name.decode(), recs[i].launches, recs[i].ms) for i in range(min(cnt.value, 32))]
 
+    def autotune(self) -> dict:
+        """One substep that also times every P2G variant and keeps the fastest (see pxf_autotune)."""
+        r = L.TuneResult()
+        _check(self._lib.pxf_autotune(self.h, C.byref(r)), self.h)
+        return _tune_dict(r)
+
     def device_bytes(self) -> int:
         return int(self._lib.pxf_device_bytes(self.h))
 
@@ -291,6 +297,11 @@ class Snapshot:
             self.h = None
 
 
+def _tune_dict(r) -> dict:
+    return {"tile_shape": r.tile_shape, "lanes": r.lanes, "chosen": r.chosen.decode(),
+            "variant_ms": [float(r.ms[i]) for i in range(min(r.variants, 16))]}
+
+
 class Batch:
     """Many simulations advanced together: one launch per stage, one CUDA graph per substep."""
 
@@ -322,6 +333,18 @@ class Batch:
 
     def sync(self) -> None:
         self._chk(self._lib.pxf_batch_sync(self.h))
+
+    def step_timed(self, n: int) -> float:
+        """Device ms of n batched substeps (CUDA events on the batch's stream)."""
+        ms = C.c_double()
+        self._chk(self._lib.pxf_batch_step_timed(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def autotune(self) -> dict:
+        """One batched substep that also picks the fastest P2G variant (see pxf_batch_autotune)."""
+        r = L.TuneResult()
+        self._chk(self._lib.pxf_batch_autotune(self.h, C.byref(r)))
+        return _tune_dict(r)
 
     def close(self):
         if self.h is not None:

@@ -79,3 +79,44 @@ def test_batch_membership_changes(lib):
     sims[1].step(0)
     for s in sims:
         s.close()
+
+
+def test_autotune_substep_is_a_normal_substep(lib):
+    """The autotuner's substep (every P2G variant timed on the sorted particles) leaves the same
+    bits as a plain substep, and later substeps with the chosen variant stay identical."""
+    spec = _specs()[1]
+    with _make(spec) as a, _make(spec) as b:
+        a.step(1)
+        r = b.autotune()
+        assert b.steps_done == 1
+        assert 0 <= r["tile_shape"] < 5 and r["lanes"] in (0, 1)
+        assert len(r["variant_ms"]) == 10 and all(m > 0 for m in r["variant_ms"])
+        assert r["variant_ms"][2 * r["tile_shape"] + r["lanes"]] == min(r["variant_ms"])
+        np.testing.assert_array_equal(a.read_particles(), b.read_particles())
+        np.testing.assert_array_equal(a.read_grid("vel"), b.read_grid("vel"))
+        a.step(3)
+        b.step(3)
+        np.testing.assert_array_equal(a.read_particles(), b.read_particles())
+
+
+def test_batch_autotune(lib):
+    specs = _specs()
+    alone = []
+    for sp in specs:
+        with _make(sp) as s:
+            s.step(3)
+            alone.append(s.read_particles())
+    sims = [_make(sp) for sp in specs]
+    b = P.Batch()
+    for s in sims:
+        b.add(s)
+    r = b.autotune()
+    assert r["chosen"].startswith("p2g ")
+    b.step(2)
+    b.sync()
+    for s, ref in zip(sims, alone):
+        assert s.steps_done == 3
+        np.testing.assert_array_equal(s.read_particles(), ref)
+    b.close()
+    for s in sims:
+        s.close()
