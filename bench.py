@@ -109,7 +109,12 @@ class ClockSampler:
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from
 # one ncu capture of this workload, keyed by (config, kernel); the capture is summarised in profiles/.
-KERNEL_TRAFFIC = {}
+KERNEL_TRAFFIC = {
+    ("dam256", "k_p2g"): 432.19e6,
+    ("dam256", "k_g2p"): 543.56e6,
+    ("dam256", "k_pcg_update"): 28.78e6,
+    ("dam256_gs", "k_pressure_rb"): 16.70e6,
+}
 
 
 def make_fluid(P, cfg):
@@ -126,17 +131,29 @@ def workload_config(name, cfg, dims, n):
             "parallelism": "replicas"}
 
 
-def kernel_bytes(kernel, N, F, C, Cf):
+def kernel_bytes(kernel, N, F, C, Cf, lv=None):
     """Algorithmic bytes of one launch of a kernel: each array the kernel must touch counted once,
-    4 B per face or cell value, 32 B per particle, 1 B per cell flag (Cf = system cells)."""
+    4 B per face or cell value, 32 B per particle, 1 B per cell flag, 2 B per neighbour record,
+    4 B per cell-list entry (Cf = system cells). Multigrid kernels: the mean over the launches of
+    one V-cycle, from the per-level system cells (lv)."""
+    if kernel in ("k_mg_smooth", "k_mg_restrict"):
+        if not lv or lv["tail"] <= 0:
+            return None
+        cf, T = lv["system_cells"], lv["tail"]
+        if kernel == "k_mg_smooth":
+            # half sweep over one colour: list, r, record in, z out (14 B per colour cell) and
+            # z of the other colour in (4 B per cell): 9 B per system cell of the level
+            return sum(9 * cf[l] for l in range(T)) / T
+        # fine r, z, record in (10 B per fine system cell); coarse list in, r and red z out
+        return sum(10 * cf[l] + 10 * cf[l + 1] for l in range(T)) / T
     return {
         "k_scan_apply": 4 * C + 4 * C + 1 * C,       # counts in; starts and cell flags out
         "k_scatter": 64 * N,                         # particle records in and out (sorted order)
         "k_p2g": 32 * N + 8 * F + 4 * C,             # sorted particles and cell starts in; vel, vel_old out
         "k_divergence": 4 * F + 1 * C + 4 * C + 2 * C,   # faces, flags in; divergence, neighbour record out
         "k_pressure_rb": 8 * C,                      # one colour: 16C per red-black iteration
-        "k_pcg_dir": 18 * Cf,                        # z, p, neighbour record in; p, Ap out
-        "k_pcg_update": 32 * Cf,                     # p, Ap, r, double-float x in; r, x out
+        "k_pcg_dir": 22 * Cf,                        # list, z, p, record in; p', Ap out
+        "k_pcg_update": 38 * Cf,                     # list, p, Ap, r, x (8 B) in; r, x, red z out
         "k_project": 8 * F + 5 * C,                  # faces in and out; pressure, flags in
         "k_g2p": 64 * N + 8 * F,                     # particles in and out; vel, vel_old in
     }.get(kernel)
@@ -457,15 +474,16 @@ def main():
         iters = sim.solver_stats()[0]
     ct = sim.read_grid("cell_type")
     Cf = int(np.count_nonzero(ct == 1))
+    lv = sim.mg_levels() if cfg["solver"] == "pcg" else None
     if not args.no_profile:
         prof = sim.profile_substep()
         total = sum(r[2] for r in prof)
         kernels = [{"kernel": n, "launches": k, "ms": m, "share": m / total} for n, k, m in prof]
         ranked = sorted(prof, key=lambda r: -r[2])
-        top = next((r for r in ranked if kernel_bytes(r[0], N, F, C, Cf)), None)
+        top = next((r for r in ranked if kernel_bytes(r[0], N, F, C, Cf, lv)), None)
         if top:
             name, launches, tot = top
-            per_launch = kernel_bytes(name, N, F, C, Cf)
+            per_launch = kernel_bytes(name, N, F, C, Cf, lv)
             achieved = per_launch / (tot / launches / 1e3) / 1e9
             roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": KERNEL_TRAFFIC.get((args.config, name)),
@@ -476,7 +494,7 @@ def main():
     achieved = B / (ms / args.steps / 1e3) / 1e9
     substep_roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "alg_bytes_per_substep": B, "pressure_iterations": iters, "system_cells": Cf,
-                        "peak_source": peak_src}
+                        "peak_source": peak_src, "mg_levels": lv}
 
     # End to end through the C ABI with pinned host buffers, one frame per step.
     e2e = None

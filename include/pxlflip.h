@@ -156,6 +156,12 @@ PXF_API int pxf_write_grid(pxf_sim* sim, int which, const void* in, size_t bytes
  * status (0 converged, 1 iteration cap, 2 breakdown, 3 zero right-hand side). */
 PXF_API int pxf_solver_stats(pxf_sim* sim, uint32_t* iterations, double* relres, uint32_t* status);
 
+/* Multigrid hierarchy of the precision solver as of the last substep: per level its cells and
+ * its system cells (fluid cells with a non-solid neighbour); *levels receives the level count,
+ * *tail the first level solved inside one block. No reference counterpart. */
+PXF_API int pxf_mg_level_info(pxf_sim* sim, uint32_t* cells, uint32_t* system_cells, uint32_t cap,
+                              uint32_t* levels, int32_t* tail);
+
 /* Device state snapshot (particles, pressure warm start, step counter). */
 PXF_API int pxf_snapshot_take(pxf_sim* sim, pxf_snapshot** out);
 PXF_API int pxf_snapshot_restore(pxf_sim* sim, const pxf_snapshot* snap);

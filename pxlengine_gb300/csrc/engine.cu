@@ -1379,6 +1379,30 @@ int pxf_solver_stats(pxf_sim* s, uint32_t* iters, double* relres, uint32_t* stat
     return PXF_OK;
 }
 
+int pxf_mg_level_info(pxf_sim* s, uint32_t* cells, uint32_t* system_cells, uint32_t cap, uint32_t* levels,
+                      int32_t* tail) {
+    if (!s || !levels || !tail) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (s->dev.solver != 1 || s->dev.precond != 0) return s->fail(PXF_ESTATE, "the simulation has no multigrid");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    *levels = uint32_t(s->dev.nlev);
+    *tail = s->dev.tail;
+    for (int l = 0; l < s->dev.nlev && uint32_t(l) < cap; l++) {
+        const MgLevel& L = s->dev.lev[l];
+        if (cells) cells[l] = L.nc;
+        if (system_cells) {
+            const uint32_t nch = (L.nc + L.cs - 1) / L.cs;
+            std::vector<uint32_t> cnt(2 * size_t(nch));
+            cudaError_t e = cudaMemcpy(cnt.data(), L.lcnt, cnt.size() * 4, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) return s->cuda_fail(e, "level lists");
+            uint64_t t = 0;
+            for (uint32_t v : cnt) t += v;
+            system_cells[l] = uint32_t(t);
+        }
+    }
+    return PXF_OK;
+}
+
 int pxf_snapshot_take(pxf_sim* s, pxf_snapshot** out) {
     if (!s || !out) return set_global_error(PXF_EINVAL, "NULL argument");
     int rc = sim_wait(s);

@@ -215,6 +215,16 @@ class FluidState:
         _check(self._lib.pxf_profile_substep(self.h, recs, 32, C.byref(cnt)), self.h)
         return [(recs[i].name.decode(), recs[i].launches, recs[i].ms) for i in range(min(cnt.value, 32))]
 
+    def mg_levels(self) -> dict:
+        """Multigrid hierarchy of the last substep: cells and system cells per level, tail level."""
+        cells = (C.c_uint32 * 16)()
+        sysc = (C.c_uint32 * 16)()
+        n = C.c_uint32()
+        tail = C.c_int32()
+        _check(self._lib.pxf_mg_level_info(self.h, cells, sysc, 16, C.byref(n), C.byref(tail)), self.h)
+        k = min(n.value, 16)
+        return {"cells": list(cells[:k]), "system_cells": list(sysc[:k]), "tail": tail.value}
+
     def autotune(self) -> dict:
         """One substep that also times every P2G variant and keeps the fastest (see pxf_autotune)."""
         r = L.TuneResult()
