@@ -45,6 +45,22 @@ CONFIGS = {
 }
 
 
+def over_ranks(dist, x, op="max"):
+    """x reduced over the ranks of the process group (identity without one)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def whole_job_rate(units_all_ranks, steps, max_ms):
+    """Particle-substeps per second of the whole job: every rank's particles times the steps, over
+    the slowest rank's time."""
+    return units_all_ranks * steps / (max_ms / 1e3)
+
+
 def env_int(k, d):
     try:
         return int(os.environ.get(k, d))
@@ -255,7 +271,7 @@ def run_batched(args, world, rank, local):
     lat = [b.step_timed(1) for _ in range(args.steps)]
     clk = clocks.stop()
     ms = sum(lat)
-    value = N * args.steps * world / (ms / 1e3)
+    value = N * args.steps / (ms / 1e3)
     div = max(divergence_linf(s) for s in sims[:4])
     iters = [s.solver_stats()[0] for s in sims]
     b.close()
@@ -271,7 +287,7 @@ def run_batched(args, world, rank, local):
     loop_value = N * loop_steps / (loop_ms / 1e3)
     for s in sims:
         s.close()
-    return {"value": value, "ms": ms, "lat": lat, "N": N, "cells": cells, "clk": clk, "tune": tune,
+    return {"value": value, "value_local": value, "ms": ms, "lat": lat, "N": N, "cells": cells, "clk": clk, "tune": tune,
             "div_linf": div, "iters": iters, "loop_value": loop_value, "loop_ms_per_round": loop_ms / loop_steps}
 
 
@@ -388,11 +404,7 @@ def main():
 
     if args.config == "batched":
         r = run_batched(args, world, rank, local)
-        if dist:
-            import torch
-            t = torch.tensor([r["ms"]], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            r["value"] = r["N"] * args.steps * world / (float(t.item()) / 1e3)
+        r["value"] = whole_job_rate(over_ranks(dist, r["N"], "sum"), args.steps, over_ranks(dist, r["ms"]))
         if rank == 0:
             line = {"metric": metric, "value": r["value"], "unit": unit, "n_gpus": world, "steps": args.steps,
                     "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
@@ -406,7 +418,7 @@ def main():
                     "plain_loop": {"value": r["loop_value"], "unit": unit,
                                    "ms_per_round": r["loop_ms_per_round"],
                                    "how": "each simulation advanced alone (own graph), one after another"},
-                    "batched_over_loop": r["value"] / world / r["loop_value"], "autotune": r["tune"],
+                    "batched_over_loop": r["value_local"] / r["loop_value"], "autotune": r["tune"],
                     "divergence_linf_dt": r["div_linf"], "pcg_iterations": [min(r["iters"]), max(r["iters"])],
                     "clocks": r["clk"], "roofline": None, "cpu_baseline": None, "e2e": None}
             print(json.dumps(line), flush=True)
@@ -450,11 +462,9 @@ def main():
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = N * args.steps * world / (ms / 1e3)
+        dist.barrier()
+    ms = over_ranks(dist, ms)
+    value = whole_job_rate(over_ranks(dist, N, "sum"), args.steps, ms)
 
     # Roofline of the dominant kernel: a kernel-by-kernel substep with a CUDA event after every
     # kernel on the library's stream (eager launches behind a hold kernel, so gaps are device time).

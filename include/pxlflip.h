@@ -196,6 +196,18 @@ typedef struct {
 } pxf_tune_result;
 PXF_API int pxf_autotune(pxf_sim* sim, pxf_tune_result* out);
 
+/* Changes the bound of the simulation's host waits (pxf_options.wait_timeout_s), e.g. a frame
+ * deadline; a wait that runs out returns PXF_ETIMEDOUT and leaves the device work running. */
+PXF_API int pxf_set_wait_timeout(pxf_sim* sim, double seconds);
+
+/* Self-test of the bounded grid barrier that the persistent precision solve uses (no reference
+ * counterpart): `rounds` barriers over `blocks` co-resident blocks of 32 threads. With skip_block
+ * >= 0 that block never arrives, so every other block's wait runs out after limit_ms (SM-clock
+ * cycles at 2.07 GHz), sets the error flag and returns; the kernel then ends normally and the
+ * context stays usable. *timed_out receives the flag (0 when every barrier completed). */
+PXF_API int pxf_selftest_grid_barrier(uint32_t blocks, int32_t skip_block, double limit_ms, uint32_t rounds,
+                                      uint32_t* timed_out);
+
 /* Selects the CUDA device of the calling host thread for the simulations it creates (the
  * library links its own CUDA runtime, so a caller's runtime setting does not carry over). */
 PXF_API int pxf_set_device(int device);

@@ -107,6 +107,8 @@ def _sig():
         "pxf_profile_substep": (C.c_int, [vp, C.POINTER(StageTime), C.c_uint32, u32p]),
         "pxf_autotune": (C.c_int, [vp, C.POINTER(TuneResult)]),
         "pxf_mg_level_info": (C.c_int, [vp, u32p, u32p, C.c_uint32, u32p, C.POINTER(C.c_int32)]),
+        "pxf_set_wait_timeout": (C.c_int, [vp, C.c_double]),
+        "pxf_selftest_grid_barrier": (C.c_int, [C.c_uint32, C.c_int32, C.c_double, C.c_uint32, u32p]),
         "pxf_set_device": (C.c_int, [C.c_int]),
         "pxf_host_alloc": (C.c_int, [C.c_size_t, pp]),
         "pxf_host_free": (None, [vp]),

@@ -1488,6 +1488,59 @@ int pxf_profile_substep(pxf_sim* s, pxf_stage_time* out, uint32_t cap, uint32_t*
     return PXF_OK;
 }
 
+int pxf_set_wait_timeout(pxf_sim* s, double seconds) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (!(seconds > 0.0)) return s->fail(PXF_EINVAL, "the wait timeout must be positive");
+    s->opts.wait_timeout_s = seconds;
+    BatchImpl* b = s->batch ? s->batch : s->own;
+    b->timeout_s = 0;
+    for (pxf_sim* m : b->sims) b->timeout_s = std::max(b->timeout_s, m->opts.wait_timeout_s);
+    if (b->sims.empty()) b->timeout_s = seconds;
+    return PXF_OK;
+}
+
+int pxf_selftest_grid_barrier(uint32_t blocks, int32_t skip_block, double limit_ms, uint32_t rounds,
+                              uint32_t* timed_out) {
+    if (!timed_out || blocks == 0 || rounds == 0 || !(limit_ms > 0.0) || limit_ms > 10000.0)
+        return set_global_error(PXF_EINVAL, "selftest: blocks, rounds > 0, 0 < limit_ms <= 10000 and an output");
+    GridBar* bar = nullptr;
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaMalloc(&bar, sizeof(GridBar));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = launch_barrier_selftest(bar, int(std::min<uint32_t>(blocks, 1u << 20)), skip_block,
+                                    (long long)(limit_ms * 2.07e6), int(std::min<uint32_t>(rounds, 1000u)), st);
+    cudaEvent_t ev = nullptr;
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) {
+        // bounded host wait: the kernel's own waits end within rounds x limit
+        const double budget = 10.0 + 2.0 * double(std::min<uint32_t>(rounds, 1000u)) * limit_ms / 1e3;
+        const auto t0 = std::chrono::steady_clock::now();
+        while ((e = cudaEventQuery(ev)) == cudaErrorNotReady) {
+            if (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > budget) break;
+            std::this_thread::sleep_for(std::chrono::microseconds(100));
+        }
+    }
+    int rc = PXF_OK;
+    if (e == cudaErrorNotReady) {
+        rc = set_global_error(PXF_ETIMEDOUT, "selftest kernel did not finish");
+    } else if (e != cudaSuccess) {
+        rc = set_global_error(PXF_ECUDA, std::string("selftest: ") + cudaGetErrorString(e));
+    } else {
+        GridBar hb;
+        e = cudaMemcpy(&hb, bar, sizeof(hb), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = set_global_error(PXF_ECUDA, std::string("selftest: ") + cudaGetErrorString(e));
+        else *timed_out = hb.err;
+    }
+    if (ev) cudaEventDestroy(ev);
+    if (rc != PXF_ETIMEDOUT) {
+        if (st) cudaStreamDestroy(st);
+        if (bar) cudaFree(bar);
+    }
+    return rc;
+}
+
 int pxf_set_device(int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) {

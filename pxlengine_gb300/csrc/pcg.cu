@@ -304,6 +304,35 @@ __device__ void ph_info(const Work& w, int l) {
 // mode 0: z = (r + sum z_n) / cnt; mode 1: the other colour is zero (z = r / cnt);
 // mode 2: as 0 with the coarse correction of level l+1 added to every neighbour on the fly
 // (fused prolongation); mode 3: as 0, then the chunk's partial r.z over all system cells.
+// One cell's update: (r + sum of its system neighbours' z, plus in mode 2 each neighbour's coarse
+// correction) / cnt.
+__device__ __forceinline__ float smooth_cell(uint32_t c, uint32_t inf, float rc, const float* __restrict__ z,
+                                             int mode, uint32_t nx, uint32_t ny, uint32_t nxy, const MgLevel& Cc,
+                                             uint32_t cnx, uint32_t cnxy) {
+    float sum = rc;
+    if (mode == 2) {
+        const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            if (!(inf & (1u << q))) continue;
+            const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+            const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+            const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+            const uint32_t n = uint32_t(int64_t(c) + dx + int64_t(dy) * nx + int64_t(dz) * nxy);
+            float zn = z[n];
+            const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
+                               cnxy * (uint32_t(int(kk) + dz) >> 1);
+            if (in_system(Cc.info[P])) zn += Cc.z[P];
+            sum += zn;
+        }
+    } else if (mode != 1) {
+#pragma unroll
+        for (int q = 0; q < 6; q++)
+            if (inf & (1u << q)) sum += z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+    }
+    return sum / cnt_of(inf);
+}
+
 __device__ void ph_smooth(const Work& w, int l, int color, int mode) {
     __shared__ double sh[32];
     for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
@@ -319,36 +348,22 @@ __device__ void ph_smooth(const Work& w, int l, int color, int mode) {
         uint32_t lo, hi;
         seg(L, chunk, color, lo, hi);
         const uint32_t* __restrict__ lst = list_of(L, chunk);
-        dep_wait();
-        if (ldu(&sp->pcg->done)) continue;
         const uint16_t* __restrict__ info = L.info;
+        // this thread's first entry and its record are fixed during the solve: read before the wait
+        const uint32_t e0 = lo + threadIdx.x;
+        const bool h0 = e0 < hi;
+        const uint32_t c0 = h0 ? __ldcg(lst + e0) : 0u;
+        const uint32_t i0 = h0 ? uint32_t(info[c0]) : 0u;
+        dep_wait();
         const float* __restrict__ r = L.r;
         float* __restrict__ z = L.z;
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
+        const uint32_t done = ldu(&sp->pcg->done);
+        const float r0 = h0 ? r[c0] : 0.0f;
+        if (done) continue;
+        if (h0) z[c0] = smooth_cell(c0, i0, r0, z, mode, nx, ny, nxy, Cc, cnx, cnxy);
+        for (uint32_t e = e0 + blockDim.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
-            const uint32_t inf = info[c];
-            float sum = r[c];
-            if (mode == 2) {
-                const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
-#pragma unroll
-                for (int q = 0; q < 6; q++) {
-                    if (!(inf & (1u << q))) continue;
-                    const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
-                    const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
-                    const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
-                    const uint32_t n = uint32_t(int64_t(c) + dx + int64_t(dy) * nx + int64_t(dz) * nxy);
-                    float zn = z[n];
-                    const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
-                                       cnxy * (uint32_t(int(kk) + dz) >> 1);
-                    if (in_system(Cc.info[P])) zn += Cc.z[P];
-                    sum += zn;
-                }
-            } else if (mode != 1) {
-#pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (inf & (1u << q)) sum += z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
-            }
-            z[c] = sum / cnt_of(inf);
+            z[c] = smooth_cell(c, info[c], r[c], z, mode, nx, ny, nxy, Cc, cnx, cnxy);
         }
         if (mode == 3) {
             // r.z over every system cell of the chunk (the other colour was final before this sweep).
@@ -714,6 +729,49 @@ __device__ void ph_resid(const Work& w) {
     }
 }
 
+// The level-0 kernels of the CG loop read each thread's first two list entries and their
+// neighbour records before dep_wait() (the lists are fixed during the solve), then issue the
+// loads of both cells together; entries beyond the first two (chunks with more than
+// 2 x 256 system cells) follow in a plain loop. The per-thread order of the reductions is the
+// list order either way.
+struct Two {
+    uint32_t e0, e1, c0, c1, i0, i1;
+    bool h0, h1;
+};
+
+__device__ __forceinline__ Two first_two(const uint32_t* lst, const uint16_t* info, uint32_t lo, uint32_t hi) {
+    Two t;
+    t.e0 = lo + threadIdx.x;
+    t.e1 = t.e0 + blockDim.x;
+    t.h0 = t.e0 < hi;
+    t.h1 = t.e1 < hi;
+    t.c0 = t.h0 ? __ldcg(lst + t.e0) : 0u;
+    t.c1 = t.h1 ? __ldcg(lst + t.e1) : 0u;
+    t.i0 = t.h0 ? uint32_t(info[t.c0]) : 0u;
+    t.i1 = t.h1 ? uint32_t(info[t.c1]) : 0u;
+    return t;
+}
+
+// p' = z + beta p (p' = z after a restart) at cell c and its six neighbours; Ap' = A p'.
+struct DirCell {
+    float pn, ap;
+};
+
+__device__ __forceinline__ DirCell dir_cell(uint32_t c, uint32_t inf, const float* __restrict__ z,
+                                            const float* __restrict__ pold, bool fresh, float beta,
+                                            int64_t nx, int64_t nxy) {
+    const float pn = fresh ? z[c] : z[c] + beta * pold[c];
+    float ap = cnt_of(inf) * pn;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        if (inf & (1u << q)) {
+            const int64_t n = int64_t(c) + nbr(q, nx, nxy);
+            ap -= fresh ? z[n] : z[n] + beta * pold[n];
+        }
+    }
+    return {pn, ap};
+}
+
 // p' = z + beta p (p' = z after a restart); Ap = A p' (neighbours' p' formed on the fly);
 // partial p'.Ap.
 __device__ void ph_dir(const Work& w) {
@@ -726,43 +784,50 @@ __device__ void ph_dir(const Work& w) {
         const uint32_t chunk = item - w.base[si];
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
+        const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
+        const uint16_t* __restrict__ info = s.info;
+        const Two t = first_two(lst, info, lo, hi);
         dep_wait();
-        if (ldu(&s.pcg->done)) continue;
         const PcgState* st = s.pcg;
+        const uint32_t done = ldu(&st->done);
         const uint32_t pbuf = ldu(&st->pbuf);
+        const bool fresh = ldu(&st->fresh) != 0;
+        const double betad = ldd(&st->beta);
+        if (done) continue;
+        const float beta = fresh ? 0.0f : float(betad);
         const float* __restrict__ pold = pbuf ? s.p1 : s.p0;
         float* __restrict__ pnew = pbuf ? s.p0 : s.p1;
         const float* __restrict__ z = s.z;
         float* __restrict__ Ap = s.Ap;
-        const uint16_t* __restrict__ info = s.info;
-        const bool fresh = ldu(&st->fresh) != 0;
-        const float beta = fresh ? 0.0f : float(ldd(&st->beta));
         const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         DF acc{0.f, 0.f};
-        const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
-#pragma unroll 2
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const uint32_t c = lst[e];
-            const uint32_t inf = info[c];
-            const float pn = fresh ? z[c] : z[c] + beta * pold[c];
-            float ap = cnt_of(inf) * pn;
-#pragma unroll
-            for (int q = 0; q < 6; q++) {
-                if (inf & (1u << q)) {
-                    const int64_t n = int64_t(c) + nbr(q, nx, nxy);
-                    ap -= fresh ? z[n] : z[n] + beta * pold[n];
-                }
-            }
-            pnew[c] = pn;
-            Ap[c] = ap;
-            acc = df_add(acc, two_prod(pn, ap));
+        DirCell d0{0.f, 0.f}, d1{0.f, 0.f};
+        if (t.h0) d0 = dir_cell(t.c0, t.i0, z, pold, fresh, beta, nx, nxy);
+        if (t.h1) d1 = dir_cell(t.c1, t.i1, z, pold, fresh, beta, nx, nxy);
+        if (t.h0) {
+            pnew[t.c0] = d0.pn;
+            Ap[t.c0] = d0.ap;
+            acc = df_add(acc, two_prod(d0.pn, d0.ap));
         }
-        const double t = block_sum(acc, sh);
-        if (threadIdx.x == 0) s.partial[chunk] = t;
+        if (t.h1) {
+            pnew[t.c1] = d1.pn;
+            Ap[t.c1] = d1.ap;
+            acc = df_add(acc, two_prod(d1.pn, d1.ap));
+        }
+        for (uint32_t e = t.e1 + blockDim.x; e < hi; e += blockDim.x) {
+            const uint32_t c = lst[e];
+            const DirCell d = dir_cell(c, info[c], z, pold, fresh, beta, nx, nxy);
+            pnew[c] = d.pn;
+            Ap[c] = d.ap;
+            acc = df_add(acc, two_prod(d.pn, d.ap));
+        }
+        const double tt = block_sum(acc, sh);
+        if (threadIdx.x == 0) s.partial[chunk] = tt;
     }
 }
 
-// x += alpha p (double-float), r -= alpha Ap (FP32), partial |r|^2.
+// x += alpha p (double-float), r -= alpha Ap (FP32), partial |r|^2; on multigrid simulations
+// also the V-cycle's first half sweep on level 0 (red from zero: z = r / cnt).
 __device__ void ph_update(const Work& w) {
     __shared__ double sh[32];
     for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
@@ -773,36 +838,46 @@ __device__ void ph_update(const Work& w) {
         const uint32_t chunk = item - w.base[si];
         uint32_t lo, hi;
         seg(s.lev[0], chunk, 2, lo, hi);
-        // The V-cycle's first half sweep on level 0 (red from zero: z = r / cnt) is done here.
         const uint32_t nred = (s.precond == 0 && s.tail > 0) ? __ldcg(s.lev[0].lcnt + 2 * chunk) : 0u;
+        const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
+        const Two t = first_two(lst, s.info, lo, hi);
         dep_wait();
-        if (ldu(&s.pcg->done)) continue;
         const PcgState* st = s.pcg;
-        const float* __restrict__ p = ldu(&st->pbuf) ? s.p1 : s.p0;
         float2* __restrict__ x2 = s.x2;
         float* __restrict__ r = s.r;
         const float* __restrict__ Ap = s.Ap;
+        float* __restrict__ z = s.lev[0].z;
+        const uint32_t done = ldu(&st->done);
+        const uint32_t pbuf = ldu(&st->pbuf);
         const float ah = ldf(&st->alpha_hi), al = ldf(&st->alpha_lo);
         const float af = float(ldd(&st->alpha));
+        // the first two cells' vectors, issued with the scalars (none depends on them)
+        float2 x0 = make_float2(0.f, 0.f), x1 = make_float2(0.f, 0.f);
+        float r0 = 0.f, r1 = 0.f, a0 = 0.f, a1 = 0.f;
+        if (t.h0) { x0 = x2[t.c0]; r0 = r[t.c0]; a0 = Ap[t.c0]; }
+        if (t.h1) { x1 = x2[t.c1]; r1 = r[t.c1]; a1 = Ap[t.c1]; }
+        if (done) continue;
+        const float* __restrict__ p = pbuf ? s.p1 : s.p0;
+        const float p0v = t.h0 ? p[t.c0] : 0.f, p1v = t.h1 ? p[t.c1] : 0.f;
         DF acc{0.f, 0.f};
-        const uint32_t* __restrict__ lst = list_of(s.lev[0], chunk);
-        float* __restrict__ z = s.lev[0].z;
-#pragma unroll 2
-        for (uint32_t e = lo + threadIdx.x; e < hi; e += blockDim.x) {
-            const uint32_t c = lst[e];
-            const float pc = p[c];
+        auto one = [&](uint32_t e, uint32_t c, uint32_t inf, float pc, float2 x, float rc, float apc) {
             DF d = two_prod(ah, pc);
             d.lo += al * pc;
-            const float2 x = x2[c];
             const DF xn = df_add(DF{x.x, x.y}, d);
             x2[c] = make_float2(xn.hi, xn.lo);
-            const float rn = r[c] - af * Ap[c];
+            const float rn = rc - af * apc;
             r[c] = rn;
-            if (e < nred) z[c] = rn / cnt_of(s.info[c]);
+            if (e < nred) z[c] = rn / cnt_of(inf);
             acc = df_add(acc, two_prod(rn, rn));
+        };
+        if (t.h0) one(t.e0, t.c0, t.i0, p0v, x0, r0, a0);
+        if (t.h1) one(t.e1, t.c1, t.i1, p1v, x1, r1, a1);
+        for (uint32_t e = t.e1 + blockDim.x; e < hi; e += blockDim.x) {
+            const uint32_t c = lst[e];
+            one(e, c, s.info[c], p[c], x2[c], r[c], Ap[c]);
         }
-        const double t = block_sum(acc, sh);
-        if (threadIdx.x == 0) s.partial[chunk] = t;
+        const double tt = block_sum(acc, sh);
+        if (threadIdx.x == 0) s.partial[chunk] = tt;
     }
 }
 
@@ -959,7 +1034,7 @@ __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
 // return to zero. Each block waits for the flip, at most kBarrierCycles; a block that gives up
 // sets `err` and every block leaves the solve at its next barrier. The launch zeroes the whole
 // GridBar, so a barrier left half-passed by an abandoned launch never reaches the next one.
-__device__ __forceinline__ bool grid_sync(GridBar* b) {
+__device__ __forceinline__ bool grid_sync(GridBar* b, long long limit = kBarrierCycles) {
     __shared__ int bad;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -969,7 +1044,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
         const unsigned old = word.fetch_add(inc, cuda::memory_order_relaxed);
         const long long t0 = clock64();
         while (((word.load(cuda::memory_order_acquire) ^ old) & 0x80000000u) == 0u) {
-            if (err.load(cuda::memory_order_relaxed) || clock64() - t0 > kBarrierCycles) {
+            if (err.load(cuda::memory_order_relaxed) || clock64() - t0 > limit) {
                 err.store(1u, cuda::memory_order_relaxed);
                 break;
             }
@@ -1198,6 +1273,37 @@ cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaS
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st) {
     k_pcg_finish<<<grid_of(pw.chunks_all.total), THREADS, 0, st>>>(mkw(pw.chunks_all)); note_launch("k_pcg_finish", st);
     return cudaGetLastError();
+}
+
+// Self-test of the grid barrier's failure path: `rounds` barriers over a cooperative grid; block
+// `skip` (if any) returns at once, so the others' waits run out after `limit` cycles, set the
+// error flag and return. Every wait is bounded, so the kernel ends either way.
+__global__ void k_barrier_selftest(GridBar* b, int skip, long long limit, int rounds) {
+    if (int(blockIdx.x) == skip) return;
+    for (int i = 0; i < rounds; i++)
+        if (!grid_sync(b, limit)) return;
+}
+
+cudaError_t launch_barrier_selftest(GridBar* bar, int blocks, int skip, long long limit, int rounds, cudaStream_t st) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_barrier_selftest, 32, 0);
+    if (e != cudaSuccess) return e;
+    const int cap = per_sm * sm_count();
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    if ((e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st)) != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(blocks));
+    cfg.blockDim = dim3(32);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_barrier_selftest, bar, skip, limit, rounds);
+    note_launch("k_barrier_selftest", st);
+    return e;
 }
 
 // Blocks of the persistent solve that are guaranteed co-resident on this device.

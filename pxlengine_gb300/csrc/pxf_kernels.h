@@ -87,6 +87,8 @@ constexpr long long kBarrierCycles = 4000000000LL;   // about 2 s at the GB300's
 // One cooperative launch that runs the whole precision solve of a substep.
 int pcg_solve_grid(size_t smem);
 constexpr int kActCounters = 1 + 2 * kMaxLevelsK;
+cudaError_t launch_barrier_selftest(GridBar* bar, int blocks, int skip, long long limit_cycles, int rounds,
+                                    cudaStream_t st);
 cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st);
 
 // Precision solver: multigrid setup + |b|^2 + state reset + first restart + first z = M^-1 r;

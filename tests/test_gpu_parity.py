@@ -171,3 +171,22 @@ def test_large_grid_properties(lib):
         assert np.all(p[:, :3] >= lo) and np.all(p[:, :3] <= hi)
         ct = s.read_grid("cell_type")
         assert np.array_equal(ct == 1, (counts > 0) & (ct != 2))
+
+
+def test_stress_double_dam_break_512(lib):
+    """512 x 256 x 256 with two boxes against opposite walls (about 95M particles, beyond the scene
+    validator's limits): conservation, finiteness and containment after two substeps."""
+    f = P.Fluid("stress", [[0, 0, 0], [2, 1, 1]],
+                [P.FluidBlock([0, 0, 0], [0.6, 0.6, 1.0]), P.FluidBlock([1.4, 0, 0], [2.0, 0.6, 1.0])],
+                resolution=512, particles_per_cell=8, substeps=8, pressure_iterations=80)
+    with P.FluidState(f, fps=15.0, options=P.make_options(lift_grid_limits=True)) as s:
+        n = s.particle_count()
+        assert s.dims == (512, 256, 256) and 94_000_000 < n < 96_500_000
+        s.step(2)
+        counts = s.read_grid("cell_count")
+        assert int(counts.sum(dtype=np.int64)) == n
+        p = s.read_particles()
+        assert np.all(np.isfinite(p))
+        h = np.float32(s.cell)
+        hi = h * (np.array([512, 256, 256], dtype=np.float32) - np.float32(1.001))
+        assert np.all(p[:, :3] >= h * np.float32(1.001)) and np.all(p[:, :3] <= hi)
