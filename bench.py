@@ -530,6 +530,17 @@ def main():
         hb_in.close()
         hb_out.close()
 
+    # Surface nets of the final particles (the meshing half of the per-frame call): device time of
+    # the second call (the first allocates the surface buffers).
+    surface = None
+    if not args.no_profile:
+        sim.surface_mesh()
+        m = sim.surface_mesh()
+        info = sim.surface_info()
+        surface = {"device_ms": m["device_ms"], "vertices": int(m["vertices"].shape[0]),
+                   "triangles": int(m["indices"].shape[0]), "overflow": m["overflow"],
+                   "surface_cells": list(info["dims"])}
+
     launches_per_substep = sum(k["launches"] for k in kernels) if kernels else None
     solver_stats = None
     if cfg["solver"] == "pcg":
@@ -550,7 +561,7 @@ def main():
                 "substep_roofline": substep_roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": (launches_per_substep * args.steps) if launches_per_substep else None,
-                "solver": solver_stats, "kernels": kernels, "wall_s_timed": t_wall}
+                "solver": solver_stats, "kernels": kernels, "surface_mesh": surface, "wall_s_timed": t_wall}
         print(json.dumps(line), flush=True)
     sim.close()
     if dist:

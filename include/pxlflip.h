@@ -148,6 +148,11 @@ PXF_API int pxf_write_particles(pxf_sim* sim, const float* in, size_t n);
 #define PXF_GRID_PRESSURE 7     /* float[C] */
 #define PXF_GRID_DIVERGENCE 8   /* float[C]  divergence before projection */
 #define PXF_GRID_PRESSURE64 9   /* double[C] FP64 pressure (precision solver only) */
+/* Surface grid of the last pxf_surface_mesh (S nodes = (sx+1)(sy+1)(sz+1), S cells = sx sy sz,
+ * s* = n* x surface_refine; fluid.slang bindings 39-41). */
+#define PXF_GRID_SURF_DENSITY 10  /* int32[S nodes]  fixed-point density x 4096 */
+#define PXF_GRID_SURF_PHI 11      /* float[S nodes]  smoothed density - iso, -1 on the boundary */
+#define PXF_GRID_SURF_CELL_VERT 12 /* uint32[S cells] vertex index or 0xffffffff */
 PXF_API int pxf_read_grid(pxf_sim* sim, int which, void* out, size_t bytes);
 /* Only PXF_GRID_PRESSURE (the warm start of the next solve) is writable. */
 PXF_API int pxf_write_grid(pxf_sim* sim, int which, const void* in, size_t bytes);
@@ -199,6 +204,28 @@ PXF_API int pxf_autotune(pxf_sim* sim, pxf_tune_result* out);
 /* Changes the bound of the simulation's host waits (pxf_options.wait_timeout_s), e.g. a frame
  * deadline; a wait that runs out returns PXF_ETIMEDOUT and leaves the device work running. */
 PXF_API int pxf_set_wait_timeout(pxf_sim* sim, double seconds);
+
+/* Surface nets of the current particles (the meshing half of Renderer::fluid_advance,
+ * crates/pxl-render/src/fluid.rs:308-330; kernels shaders/fluid.slang:222-355): density splat,
+ * smoothing, vertices and quads into device buffers the library owns (allocated on the first
+ * call: about 12 bytes per surface node and cell plus max_triangles x 44 bytes). Returns the
+ * counts the reference reads back, capped like the reference (vertices <= max_triangles,
+ * triangles <= max_triangles, even), and the overflow flag (fluid.rs:324-327). Vertices are
+ * numbered by ascending surface cell and triangles by ascending node and axis (the reference's
+ * order follows its atomic counters and varies from run to run). device_ms (optional) receives
+ * the meshing's device time. */
+PXF_API int pxf_surface_mesh(pxf_sim* sim, uint32_t* vertices, uint32_t* triangles, int32_t* overflow,
+                             double* device_ms);
+/* Surface grid of the simulation as FluidState::new sets it (fluid.rs:150-156): surface cells per
+ * axis (grid cells x surface_refine), surface cell size, splat radius and iso level. */
+PXF_API int pxf_surface_info(const pxf_sim* sim, uint32_t dims[3], float* cell, float* radius, float* iso);
+/* Copies the mesh of the last pxf_surface_mesh: vertices as [x, y, z, 0, nx, ny, nz, 0] records
+ * (the renderer's vertex layout), triangles as three vertex indices; n_vertices / n_triangles must
+ * equal the counts pxf_surface_mesh returned. */
+PXF_API int pxf_read_mesh(pxf_sim* sim, float* vertices, size_t n_vertices, uint32_t* indices, size_t n_triangles);
+/* Device addresses of the mesh buffers (valid until the next pxf_surface_mesh or pxf_destroy),
+ * for consumers that build acceleration structures or render from device memory directly. */
+PXF_API int pxf_mesh_device_buffers(pxf_sim* sim, const void** vertices, const void** indices);
 
 /* Self-test of the bounded grid barrier that the persistent precision solve uses (no reference
  * counterpart): `rounds` barriers over `blocks` co-resident blocks of 32 threads. With skip_block

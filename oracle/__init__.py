@@ -6,3 +6,4 @@ timed CPU baseline. Never imported by the pxlengine_gb300 package.
 from .oracle import (PARTICLES, VEL, VEL_OLD, ACC, WACC, CELL_COUNT, CELL_TYPE, PRESSURE,  # noqa: F401
                      DIVERGENCE, PRESSURE64, STAGES)
 from .oracle import OracleSim, grid, lcg, seed_particles, steps_for_frame, dt_for, num_threads, load  # noqa: F401
+from .oracle import surface_nets  # noqa: F401

@@ -13,6 +13,8 @@
 //   crates/pxl-render/src/fluid.rs:234-236  steps_for_frame
 //   crates/pxl-render/src/fluid.rs:289-303  substep schedule
 //   crates/pxl-scene/src/lib.rs:121-129     Fluid::grid
+//   shaders/fluid.slang:222-355       surface nets: s_clear, s_splat, s_phi, s_verts, s_quads
+//   crates/pxl-render/src/fluid.rs:150-156, 308-330  surface grid, iso level, meshing schedule
 //
 // Parity status: partially pinned. The reference ships no numeric golden vectors and its
 // Slang/Vulkan path cannot run on these machines (no slangc, no Vulkan loader, no Rust
@@ -844,6 +846,152 @@ int orc_sim_step(void* p, uint32_t n) {
     for (uint32_t i = 0; i < n; i++) {
         if (hd->dbl) hd->d->substep(); else hd->f->substep();
     }
+    return 0;
+}
+
+// Surface nets of particles[n] (AoS, 8 floats each) on a surface grid of sdims cells (nodes one
+// more per axis). Vertices are numbered by ascending surface cell, triangles by ascending node and
+// axis (a serial order; the reference's follows its atomic counters). Outputs: density and phi per
+// node, cell_vert per cell, verts[max_verts][8], indices[max_tris][3], counts = {vertices,
+// triangles} before the caps.
+int orc_surface_nets(const float* particles, int64_t n, const uint32_t sdims[3], float sh, float radius, float iso,
+                     const float origin[3], uint32_t max_verts, uint32_t max_tris, int32_t* density, float* phi,
+                     uint32_t* cell_vert, float* verts, uint32_t* indices, uint32_t counts[2]) {
+    const int X = int(sdims[0]), Y = int(sdims[1]), Z = int(sdims[2]);
+    const int64_t NX = X + 1, NY = Y + 1, nn = NX * NY * (Z + 1), nc = int64_t(X) * Y * Z;
+    const float SD = 4096.0f;
+    const uint32_t NONE = 0xffffffffu;
+    auto node = [&](int i, int j, int k) { return int64_t(i) + NX * (int64_t(j) + NY * int64_t(k)); };
+    // s_clear
+    std::fill(density, density + nn, 0);
+    // s_splat (integer sums: the order of the additions does not matter)
+    const float r = radius / sh;
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < n; p++) {
+        const float* P = particles + 8 * p;
+        const float gx = (P[0] - origin[0]) / sh, gy = (P[1] - origin[1]) / sh, gz = (P[2] - origin[2]) / sh;
+        const int lx = std::max(to_i32(std::ceil(gx - r)), 0), ly = std::max(to_i32(std::ceil(gy - r)), 0),
+                  lz = std::max(to_i32(std::ceil(gz - r)), 0);
+        const int hx = std::min(to_i32(std::floor(gx + r)), X), hy = std::min(to_i32(std::floor(gy + r)), Y),
+                  hz = std::min(to_i32(std::floor(gz + r)), Z);
+        for (int k = lz; k <= hz; k++)
+            for (int j = ly; j <= hy; j++)
+                for (int i = lx; i <= hx; i++) {
+                    const float dx = float(i) - gx, dy = float(j) - gy, dz = float(k) - gz;
+                    const float q = 1.0f - (dx * dx + dy * dy + dz * dz) / (r * r);
+                    if (q > 0.0f) {
+                        const int32_t add = to_i32(q * q * q * SD);
+                        int32_t* d = density + node(i, j, k);
+#pragma omp atomic
+                        *d += add;
+                    }
+                }
+    }
+    // s_phi
+#pragma omp parallel for schedule(static)
+    for (int64_t id = 0; id < nn; id++) {
+        const int i = int(id % NX), j = int((id / NX) % NY), k = int(id / (NX * NY));
+        float sum = 2.0f * float(density[id]);
+        float wsum = 2.0f;
+        for (int a = 0; a < 6; a++) {
+            int q[3] = {i, j, k};
+            q[a >> 1] += (a & 1) ? 1 : -1;
+            if (q[0] < 0 || q[1] < 0 || q[2] < 0 || q[0] > X || q[1] > Y || q[2] > Z) continue;
+            sum += float(density[node(q[0], q[1], q[2])]);
+            wsum += 1.0f;
+        }
+        const bool edge = i == 0 || j == 0 || k == 0 || i == X || j == Y || k == Z;
+        phi[id] = edge ? -1.0f : sum / wsum / SD - iso;
+    }
+    // s_verts, serially in cell order
+    uint32_t nv = 0;
+    for (int64_t c = 0; c < nc; c++) {
+        const int ci = int(c % X), cj = int((c / X) % Y), ck = int(c / (int64_t(X) * Y));
+        float v[8];
+        uint32_t inside = 0;
+        for (int q = 0; q < 8; q++) {
+            v[q] = phi[node(ci + (q & 1), cj + ((q >> 1) & 1), ck + (q >> 2))];
+            if (v[q] > 0.0f) inside |= 1u << q;
+        }
+        cell_vert[c] = NONE;
+        if (inside == 0 || inside == 255) continue;
+        const uint32_t idx = nv++;
+        if (idx >= max_verts) continue;
+        float sx = 0, sy = 0, sz = 0, cnt = 0;
+        for (int e = 0; e < 12; e++) {
+            const int axis = e >> 2, bits = e & 3, o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
+            int a0 = 0;
+            if (bits & 1) a0 |= 1 << o1;
+            if (bits & 2) a0 |= 1 << o2;
+            const int a1 = a0 | (1 << axis);
+            if ((v[a0] > 0.0f) == (v[a1] > 0.0f)) continue;
+            const float t = v[a0] / (v[a0] - v[a1]);
+            sx += fmix(float(a0 & 1), float(a1 & 1), t);
+            sy += fmix(float((a0 >> 1) & 1), float((a1 >> 1) & 1), t);
+            sz += fmix(float(a0 >> 2), float(a1 >> 2), t);
+            cnt += 1.0f;
+        }
+        const float lx = sx / cnt, ly = sy / cnt, lz = sz / cnt;
+        float gx = 0, gy = 0, gz = 0;
+        for (int k = 0; k < 8; k++) {
+            const bool ox = k & 1, oy = (k >> 1) & 1, oz = k >> 2;
+            const float wx = ox ? lx : 1.0f - lx, wy = oy ? ly : 1.0f - ly, wz = oz ? lz : 1.0f - lz;
+            const float qx = ox ? 1.0f : -1.0f, qy = oy ? 1.0f : -1.0f, qz = oz ? 1.0f : -1.0f;
+            gx += v[k] * (qx * wy * wz);
+            gy += v[k] * (qy * wx * wz);
+            gz += v[k] * (qz * wx * wy);
+        }
+        gx = gx + 0.0f;
+        gy = gy + 1e-9f;
+        gz = gz + 0.0f;
+        const float len = std::sqrt(gx * gx + gy * gy + gz * gz);
+        float* o = verts + 8 * size_t(idx);
+        o[0] = origin[0] + (float(ci) + lx) * sh;
+        o[1] = origin[1] + (float(cj) + ly) * sh;
+        o[2] = origin[2] + (float(ck) + lz) * sh;
+        o[3] = 0.0f;
+        o[4] = -(gx / len);
+        o[5] = -(gy / len);
+        o[6] = -(gz / len);
+        o[7] = 0.0f;
+        cell_vert[c] = idx;
+    }
+    // s_quads, serially in node order, then axis
+    uint32_t nq = 0;
+    const int lim[3] = {X, Y, Z};
+    for (int64_t id = 0; id < nn; id++) {
+        const int nd[3] = {int(id % NX), int((id / NX) % NY), int(id / (NX * NY))};
+        const bool in0 = phi[id] > 0.0f;
+        for (int axis = 0; axis < 3; axis++) {
+            int m[3] = {nd[0], nd[1], nd[2]};
+            m[axis] += 1;
+            if (m[axis] > lim[axis]) continue;
+            if (in0 == (phi[node(m[0], m[1], m[2])] > 0.0f)) continue;
+            const int o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
+            const int offs[4][2] = {{-1, -1}, {0, -1}, {0, 0}, {-1, 0}};
+            uint32_t q[4];
+            bool ok = true;
+            for (int k = 0; k < 4 && ok; k++) {
+                int c[3] = {nd[0], nd[1], nd[2]};
+                c[o1] += offs[k][0];
+                c[o2] += offs[k][1];
+                if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= X || c[1] >= Y || c[2] >= Z) { ok = false; break; }
+                q[k] = cell_vert[int64_t(c[0]) + int64_t(X) * (int64_t(c[1]) + int64_t(Y) * c[2])];
+                if (q[k] == NONE) ok = false;
+            }
+            if (!ok) continue;
+            const uint32_t t = 2 * nq++;
+            if (t + 2 > max_tris) continue;
+            uint32_t* b = indices + size_t(t) * 3;
+            if (in0) {
+                b[0] = q[0]; b[1] = q[1]; b[2] = q[2]; b[3] = q[0]; b[4] = q[2]; b[5] = q[3];
+            } else {
+                b[0] = q[0]; b[1] = q[2]; b[2] = q[1]; b[3] = q[0]; b[4] = q[3]; b[5] = q[2];
+            }
+        }
+    }
+    counts[0] = nv;
+    counts[1] = 2 * nq;
     return 0;
 }
 

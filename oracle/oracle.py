@@ -46,6 +46,9 @@ def load():
     lib.orc_sim_step.argtypes = [C.c_void_p, C.c_uint32]
     lib.orc_sim_read.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
     lib.orc_sim_write.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]
+    lib.orc_surface_nets.argtypes = [C.c_void_p, C.c_int64, u32p, C.c_float, C.c_float, C.c_float, f32p,
+                                     C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, u32p]
     _lib = lib
     return lib
 
@@ -88,6 +91,31 @@ def seed_particles(bounds, resolution, fill, ppc, seed):
     out = np.zeros((n, 8), dtype=np.float32)
     lib.orc_seed(bp, resolution, fp, len(rows), ppc, seed, out.ctypes.data_as(C.POINTER(C.c_float)), n)
     return out
+
+
+def surface_nets(particles, sdims, sh, radius, iso, origin, max_verts, max_tris):
+    """Surface nets of particles ([N, 8] float32) on a surface grid of sdims cells
+    (shaders/fluid.slang:222-355); vertices in ascending cell order, triangles in ascending node
+    and axis order. Returns density, phi, cell_vert, vertices [V, 8], indices [T, 3] and the
+    uncapped counts."""
+    lib = load()
+    p = np.ascontiguousarray(particles, dtype=np.float32).reshape(-1, 8)
+    sx, sy, sz = (int(v) for v in sdims)
+    nn, nc = (sx + 1) * (sy + 1) * (sz + 1), sx * sy * sz
+    den = np.empty(nn, dtype=np.int32)
+    phi = np.empty(nn, dtype=np.float32)
+    cv = np.empty(nc, dtype=np.uint32)
+    verts = np.zeros((max_verts, 8), dtype=np.float32)
+    idx = np.zeros((max_tris, 3), dtype=np.uint32)
+    cnt = (C.c_uint32 * 2)()
+    d = (C.c_uint32 * 3)(sx, sy, sz)
+    o = (C.c_float * 3)(*[float(v) for v in origin])
+    lib.orc_surface_nets(p.ctypes.data, p.shape[0], d, float(sh), float(radius), float(iso), o, int(max_verts),
+                         int(max_tris), den.ctypes.data, phi.ctypes.data, cv.ctypes.data, verts.ctypes.data,
+                         idx.ctypes.data, cnt)
+    nv, nt = min(cnt[0], max_verts), min(cnt[1], max_tris) // 2 * 2
+    return {"density": den, "phi": phi, "cell_vert": cv, "vertices": verts[:nv], "indices": idx[:nt],
+            "counts": (cnt[0], cnt[1])}
 
 
 def steps_for_frame(warmup, fps, substeps, frame):

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libpxlflip.so")
 PXF_OK, PXF_EINVAL, PXF_ECUDA, PXF_ENOMEM, PXF_ETIMEDOUT, PXF_ESTATE, PXF_ENOTFOUND = 0, -1, -2, -3, -4, -5, -6
 PXF_PRESSURE_RBGS, PXF_PRESSURE_PCG = 0, 1
 GRID = {"vel": 1, "vel_old": 2, "acc": 3, "wacc": 4, "cell_count": 5, "cell_type": 6, "pressure": 7,
-        "divergence": 8, "pressure64": 9}
+        "divergence": 8, "pressure64": 9, "surf_density": 10, "surf_phi": 11, "surf_cell_vert": 12}
 
 # Every exported function and its (restype, argtypes); the not-GPU tests check this list against
 # the header and the library's dynamic symbol table.
@@ -108,6 +108,10 @@ def _sig():
         "pxf_autotune": (C.c_int, [vp, C.POINTER(TuneResult)]),
         "pxf_mg_level_info": (C.c_int, [vp, u32p, u32p, C.c_uint32, u32p, C.POINTER(C.c_int32)]),
         "pxf_set_wait_timeout": (C.c_int, [vp, C.c_double]),
+        "pxf_surface_mesh": (C.c_int, [vp, u32p, u32p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+        "pxf_read_mesh": (C.c_int, [vp, vp, C.c_size_t, vp, C.c_size_t]),
+        "pxf_surface_info": (C.c_int, [vp, u32p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+        "pxf_mesh_device_buffers": (C.c_int, [vp, pp, pp]),
         "pxf_selftest_grid_barrier": (C.c_int, [C.c_uint32, C.c_int32, C.c_double, C.c_uint32, u32p]),
         "pxf_set_device": (C.c_int, [C.c_int]),
         "pxf_host_alloc": (C.c_int, [C.c_size_t, pp]),

@@ -24,6 +24,7 @@
 #include "../../include/pxlflip.h"
 #include "engine.h"
 #include "pxf_device.cuh"
+#include "surface.h"
 #include "pxf_kernels.h"
 #include "scene.h"
 #include "seed.h"
@@ -129,6 +130,9 @@ struct pxf_sim {
     bool initialized = false;
     pxf::BatchImpl* batch = nullptr;      // batch that steps this simulation
     pxf::BatchImpl* own = nullptr;        // private batch of one
+    void* surf_mem = nullptr;             // surface grid + mesh buffers (first pxf_surface_mesh)
+    pxf::SurfDev surf{};
+    uint32_t mesh_verts = 0, mesh_tris = 0;   // capped counts of the last mesh
     std::string err;
 
     int fail(int code, const std::string& m) { err = m; return code; }
@@ -1333,11 +1337,146 @@ int pxf_read_grid(pxf_sim* s, int which, void* out, size_t bytes) {
             if (!need(8ull * d.nc)) return s->fail(PXF_EINVAL, "size mismatch");
             e = cudaMemcpyAsync(out, d.x64, bytes, cudaMemcpyDeviceToHost, st);
             break;
+        case PXF_GRID_SURF_DENSITY:
+        case PXF_GRID_SURF_PHI:
+        case PXF_GRID_SURF_CELL_VERT: {
+            if (!s->surf_mem) return s->fail(PXF_ESTATE, "no surface mesh has been made yet");
+            const SurfDev& S = s->surf;
+            const size_t nn = size_t(S.sx + 1) * (S.sy + 1) * (S.sz + 1), sc = size_t(S.sx) * S.sy * S.sz;
+            const size_t want = 4 * (which == PXF_GRID_SURF_CELL_VERT ? sc : nn);
+            if (!need(want)) return s->fail(PXF_EINVAL, "size mismatch");
+            const void* src = which == PXF_GRID_SURF_DENSITY ? static_cast<const void*>(S.density)
+                              : which == PXF_GRID_SURF_PHI  ? static_cast<const void*>(S.phi)
+                                                            : static_cast<const void*>(S.cell_vert);
+            e = cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, st);
+            break;
+        }
         default:
             return s->fail(PXF_EINVAL, "unknown grid buffer");
     }
     if (e != cudaSuccess) return s->cuda_fail(e, "read grid");
     return sim_wait(s);
+}
+
+// Surface grid and iso level as FluidState::new sets them (fluid.rs:150-156); powi(3) is x*x*x.
+static SurfDev surface_params(const pxf_sim* s) {
+    const FluidCfg& f = s->cfg;
+    SurfDev S{};
+    const uint32_t r = f.surface_refine;
+    S.sx = s->dims[0] * r;
+    S.sy = s->dims[1] * r;
+    S.sz = s->dims[2] * r;
+    S.sh = s->h / float(r);
+    S.radius = f.particle_radius * S.sh;
+    const float x = S.radius / s->h;
+    const float kernel_volume = 0.638f * (x * x * x);
+    S.iso = 0.5f * float(f.particles_per_cell) * kernel_volume;
+    S.ox = s->dev.o[0];
+    S.oy = s->dev.o[1];
+    S.oz = s->dev.o[2];
+    S.max_verts = f.max_triangles;
+    S.max_tris = f.max_triangles;
+    return S;
+}
+
+int pxf_surface_info(const pxf_sim* s, uint32_t dims[3], float* cell, float* radius, float* iso) {
+    if (!s || !dims) return set_global_error(PXF_EINVAL, "NULL argument");
+    const SurfDev S = surface_params(s);
+    dims[0] = S.sx;
+    dims[1] = S.sy;
+    dims[2] = S.sz;
+    if (cell) *cell = S.sh;
+    if (radius) *radius = S.radius;
+    if (iso) *iso = S.iso;
+    return PXF_OK;
+}
+
+int pxf_surface_mesh(pxf_sim* s, uint32_t* vertices, uint32_t* triangles, int32_t* overflow, double* device_ms) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    const FluidCfg& f = s->cfg;
+    if (f.surface_refine == 0) return s->fail(PXF_EINVAL, "surface_refine must be at least 1");
+    cudaError_t e;
+    if (!s->surf_mem) {
+        SurfDev S = surface_params(s);
+        const uint64_t nn = uint64_t(S.sx + 1) * (S.sy + 1) * (S.sz + 1), sc = uint64_t(S.sx) * S.sy * S.sz;
+        if (nn >= (1ull << 32)) return s->fail(PXF_EINVAL, "surface grid too large (2^32 nodes)");
+        size_t off = 0;
+        auto take = [&](size_t b) { const size_t o = off; off += align256(b); return o; };
+        const size_t o_den = take(4 * nn), o_phi = take(4 * nn), o_cv = take(4 * sc);
+        const size_t o_v = take(size_t(S.max_verts) * 32), o_i = take(size_t(S.max_tris) * 12);
+        const size_t o_vc = take(4 * size_t(surface_chunks(sc))), o_qc = take(4 * size_t(surface_chunks(nn)));
+        const size_t o_ct = take(16);
+        void* mem = nullptr;
+        if ((e = cudaMalloc(&mem, off)) != cudaSuccess) {
+            cudaGetLastError();
+            return s->fail(PXF_ENOMEM, "surface buffers: " + std::to_string(off) + " bytes");
+        }
+        char* b = static_cast<char*>(mem);
+        S.density = reinterpret_cast<int32_t*>(b + o_den);
+        S.phi = reinterpret_cast<float*>(b + o_phi);
+        S.cell_vert = reinterpret_cast<uint32_t*>(b + o_cv);
+        S.verts = reinterpret_cast<float4*>(b + o_v);
+        S.indices = reinterpret_cast<uint32_t*>(b + o_i);
+        S.vchunk = reinterpret_cast<uint32_t*>(b + o_vc);
+        S.qchunk = reinterpret_cast<uint32_t*>(b + o_qc);
+        S.counters = reinterpret_cast<uint32_t*>(b + o_ct);
+        s->surf_mem = mem;
+        s->surf = S;
+    }
+    cudaStream_t st = sim_stream(s);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    e = launch_surface(s->surf, s->dev.posA, s->dev.np, st);
+    cudaEventRecord(e1, st);
+    if (e != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return s->cuda_fail(e, "surface launch");
+    }
+    rc = sim_wait(s);
+    float ms = 0;
+    if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    uint32_t cnt[2] = {0, 0};
+    if ((e = cudaMemcpy(cnt, s->surf.counters, 8, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return s->cuda_fail(e, "surface counters");
+    const uint32_t mv = s->surf.max_verts, mt = s->surf.max_tris;
+    s->mesh_verts = std::min(cnt[0], mv);
+    s->mesh_tris = std::min(cnt[1], mt) / 2 * 2;
+    if (vertices) *vertices = s->mesh_verts;
+    if (triangles) *triangles = s->mesh_tris;
+    if (overflow) *overflow = (cnt[0] > mv || cnt[1] > mt) ? 1 : 0;
+    if (device_ms) *device_ms = ms;
+    return PXF_OK;
+}
+
+int pxf_read_mesh(pxf_sim* s, float* vertices, size_t n_vertices, uint32_t* indices, size_t n_triangles) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (!s->surf_mem) return s->fail(PXF_ESTATE, "no surface mesh has been made yet");
+    if (n_vertices != s->mesh_verts || n_triangles != s->mesh_tris)
+        return s->fail(PXF_EINVAL, "counts differ from the last pxf_surface_mesh");
+    if ((n_vertices && !vertices) || (n_triangles && !indices)) return s->fail(PXF_EINVAL, "NULL buffer");
+    int rc = sim_wait(s);
+    if (rc) return rc;
+    cudaError_t e = cudaSuccess;
+    if (n_vertices) e = cudaMemcpy(vertices, s->surf.verts, n_vertices * 32, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && n_triangles) e = cudaMemcpy(indices, s->surf.indices, n_triangles * 12, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return s->cuda_fail(e, "read mesh");
+    return PXF_OK;
+}
+
+int pxf_mesh_device_buffers(pxf_sim* s, const void** vertices, const void** indices) {
+    if (!s || !vertices || !indices) return set_global_error(PXF_EINVAL, "NULL argument");
+    if (!s->surf_mem) return s->fail(PXF_ESTATE, "no surface mesh has been made yet");
+    *vertices = s->surf.verts;
+    *indices = s->surf.indices;
+    return PXF_OK;
 }
 
 int pxf_write_grid(pxf_sim* s, int which, const void* in, size_t bytes) {
@@ -1578,6 +1717,7 @@ void pxf_destroy(pxf_sim* s) {
         delete s->own;
     }
     if (s->mem) cudaFree(s->mem);
+    if (s->surf_mem) cudaFree(s->surf_mem);
     delete s;
 }
 

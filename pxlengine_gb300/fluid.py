@@ -125,7 +125,8 @@ def _check(rc: int, handle=None):
 
 _GRID_DTYPES = {"vel": np.float32, "vel_old": np.float32, "acc": np.int32, "wacc": np.int32,
                 "cell_count": np.uint32, "cell_type": np.uint32, "pressure": np.float32,
-                "divergence": np.float32, "pressure64": np.float64}
+                "divergence": np.float32, "pressure64": np.float64, "surf_density": np.int32,
+                "surf_phi": np.float32, "surf_cell_vert": np.uint32}
 
 
 class FluidState:
@@ -215,6 +216,25 @@ class FluidState:
         _check(self._lib.pxf_profile_substep(self.h, recs, 32, C.byref(cnt)), self.h)
         return [(recs[i].name.decode(), recs[i].launches, recs[i].ms) for i in range(min(cnt.value, 32))]
 
+    def surface_info(self) -> dict:
+        """Surface grid (pxf_surface_info): cells per axis, cell size, splat radius, iso level."""
+        d = (C.c_uint32 * 3)()
+        cell, rad, iso = C.c_float(), C.c_float(), C.c_float()
+        _check(self._lib.pxf_surface_info(self.h, d, C.byref(cell), C.byref(rad), C.byref(iso)), self.h)
+        return {"dims": (d[0], d[1], d[2]), "cell": cell.value, "radius": rad.value, "iso": iso.value}
+
+    def surface_mesh(self) -> dict:
+        """Surface nets of the current particles (pxf_surface_mesh): vertices [V, 8] float32
+        ([x, y, z, 0, nx, ny, nz, 0]), indices [T, 3] uint32, overflow flag, device ms."""
+        nv, nt = C.c_uint32(), C.c_uint32()
+        ov = C.c_int32()
+        ms = C.c_double()
+        _check(self._lib.pxf_surface_mesh(self.h, C.byref(nv), C.byref(nt), C.byref(ov), C.byref(ms)), self.h)
+        verts = np.empty((nv.value, 8), dtype=np.float32)
+        idx = np.empty((nt.value, 3), dtype=np.uint32)
+        _check(self._lib.pxf_read_mesh(self.h, verts.ctypes.data, nv.value, idx.ctypes.data, nt.value), self.h)
+        return {"vertices": verts, "indices": idx, "overflow": bool(ov.value), "device_ms": ms.value}
+
     def mg_levels(self) -> dict:
         """Multigrid hierarchy of the last substep: cells and system cells per level, tail level."""
         cells = (C.c_uint32 * 16)()
@@ -248,6 +268,9 @@ class FluidState:
     def read_grid(self, name: str) -> np.ndarray:
         dt = _GRID_DTYPES[name]
         n = self.n_faces if name in ("vel", "vel_old", "acc", "wacc") else self.n_cells
+        if name.startswith("surf_"):
+            sx, sy, sz = self.surface_info()["dims"]
+            n = sx * sy * sz if name == "surf_cell_vert" else (sx + 1) * (sy + 1) * (sz + 1)
         out = np.empty(n, dtype=dt)
         _check(self._lib.pxf_read_grid(self.h, L.GRID[name], out.ctypes.data, out.nbytes), self.h)
         return out
