@@ -102,6 +102,7 @@ struct BatchImpl {
     int record_post(cudaStream_t st);
     int record_gs_part(cudaStream_t st);     // scan .. divergence and the red-black sweeps
     int record_post_solve(cudaStream_t st);  // project, g2p
+    cudaError_t record_gs(cudaStream_t st);  // the red-black sweeps
     int step(uint32_t n);
     int wait();
     void drop_graphs();
@@ -207,6 +208,9 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
     L.info = take(2 * nc);
     L.acc = o.keep_p2g_sums ? take(4 * nf) : 0;
     L.wacc = o.keep_p2g_sums ? take(4 * nf) : 0;
+    // level-0 system-cell lists (red then black per chunk): both pressure solvers walk them
+    L.llist[0] = take(4 * nchunks * kScanChunk);
+    L.llcnt[0] = take(8 * nchunks);
     const bool pcg = o.pressure_solver == PXF_PRESSURE_PCG;
     if (pcg) {
         L.x2 = take(8 * nc);
@@ -218,8 +222,6 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
         L.Ap = take(4 * nc);
         L.partial = take(8 * nchunks);
         L.pcg = take(sizeof(PcgState));
-        L.llist[0] = take(4 * nchunks * kScanChunk);
-        L.llcnt[0] = take(8 * nchunks);
         if (o.pcg_precond == 0) {
             L.nlev = mg_levels(n, L.dims);
             for (int l = 1; l < L.nlev; l++) {
@@ -472,12 +474,22 @@ int BatchImpl::record_gs_part(cudaStream_t st) {
     if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
     if ((e = launch_p2g(w_tiles, tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
     if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
-    if (any_gs) {
-        for (uint32_t it = 0; it < max_gs_iters; it++)
-            for (uint32_t parity = 0; parity < 2; parity++)
-                if ((e = launch_pressure_rb(w_half, parity, it, st)) != cudaSuccess) return cuda_fail(e, "pressure");
-    }
+    if (any_gs && (e = record_gs(st)) != cudaSuccess) return cuda_fail(e, "pressure");
     return PXF_OK;
+}
+
+// The reference red-black GS: 2 x iterations launches over the level-0 system-cell lists (built
+// once per substep), or, with PXF_GS_DENSE=1, over every cell of one colour.
+cudaError_t BatchImpl::record_gs(cudaStream_t st) {
+    static const bool dense = [] { const char* v = std::getenv("PXF_GS_DENSE"); return v && v[0] == '1'; }();
+    cudaError_t e = cudaSuccess;
+    if (!dense && (e = launch_gs_lists(w_chunks, st)) != cudaSuccess) return e;
+    for (uint32_t it = 0; it < max_gs_iters; it++)
+        for (uint32_t parity = 0; parity < 2; parity++) {
+            e = dense ? launch_pressure_rb(w_half, parity, it, st) : launch_pressure_rb_list(w_chunks, parity, it, st);
+            if (e != cudaSuccess) return e;
+        }
+    return e;
 }
 
 int BatchImpl::record_post_solve(cudaStream_t st) {
@@ -494,11 +506,7 @@ int BatchImpl::record_pre(cudaStream_t st) {
     if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
     if ((e = launch_p2g(w_tiles, tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
     if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
-    if (any_gs) {
-        for (uint32_t it = 0; it < max_gs_iters; it++)
-            for (uint32_t parity = 0; parity < 2; parity++)
-                if ((e = launch_pressure_rb(w_half, parity, it, st)) != cudaSuccess) return cuda_fail(e, "pressure");
-    }
+    if (any_gs && (e = record_gs(st)) != cudaSuccess) return cuda_fail(e, "pressure");
     if (any_pcg && (e = launch_pcg_init(pw, st)) != cudaSuccess) return cuda_fail(e, "pcg init");
     return PXF_OK;
 }
@@ -824,11 +832,7 @@ int BatchImpl::run_eager(KernelTimer* timer, pxf_tune_result* tune) {
         return cuda_fail(e, "p2g");
     }
     if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
-    if (any_gs) {
-        for (uint32_t it = 0; it < max_gs_iters; it++)
-            for (uint32_t parity = 0; parity < 2; parity++)
-                if ((e = launch_pressure_rb(w_half, parity, it, stream)) != cudaSuccess) return cuda_fail(e, "pressure");
-    }
+    if (any_gs && (e = record_gs(stream)) != cudaSuccess) return cuda_fail(e, "pressure");
     if (any_pcg && persistent) {
         if ((e = launch_pcg_solve(pw, d_bar, persist_grid, persist_guard, stream)) != cudaSuccess)
             return cuda_fail(e, "pcg solve");
@@ -1035,6 +1039,13 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.info = reinterpret_cast<uint16_t*>(m + L.info);
     d.acc = opts.keep_p2g_sums ? reinterpret_cast<int32_t*>(m + L.acc) : nullptr;
     d.wacc = opts.keep_p2g_sums ? reinterpret_cast<int32_t*>(m + L.wacc) : nullptr;
+    d.lev[0].nx = d.nx; d.lev[0].ny = d.ny; d.lev[0].nz = d.nz;
+    d.lev[0].nc = d.nc;
+    d.lev[0].type = d.type;
+    d.lev[0].info = d.info;
+    d.lev[0].cs = kScanChunk;
+    d.lev[0].list = reinterpret_cast<uint32_t*>(m + L.llist[0]);
+    d.lev[0].lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[0]);
     if (opts.pressure_solver == PXF_PRESSURE_PCG) {
         d.x2 = reinterpret_cast<float2*>(m + L.x2);
         d.x64 = reinterpret_cast<double*>(m + L.x64);
@@ -1048,15 +1059,8 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
         d.nlev = L.nlev > 0 ? L.nlev : 1;
         d.tail = 0;
         while (d.tail + 1 < d.nlev && uint64_t(L.dims[d.tail][0]) * L.dims[d.tail][1] * L.dims[d.tail][2] > kTailCells) d.tail++;
-        d.lev[0].nx = d.nx; d.lev[0].ny = d.ny; d.lev[0].nz = d.nz;
-        d.lev[0].nc = d.nc;
-        d.lev[0].type = d.type;
-        d.lev[0].info = d.info;
         d.lev[0].r = d.r;
         d.lev[0].z = d.z;
-        d.lev[0].cs = kScanChunk;
-        d.lev[0].list = reinterpret_cast<uint32_t*>(m + L.llist[0]);
-        d.lev[0].lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[0]);
         for (int l = 1; l < L.nlev; l++) {
             MgLevel& v = d.lev[l];
             v.nx = L.dims[l][0]; v.ny = L.dims[l][1]; v.nz = L.dims[l][2];

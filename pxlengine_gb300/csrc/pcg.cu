@@ -154,13 +154,13 @@ __device__ __forceinline__ void dep_wait() {
 // kernels and the persistent kernel.
 
 // Compacts each chunk of level l into its red then black system cells, in ascending cell order.
-__device__ void ph_cell_lists(const Work& w, int l) {
+__device__ void ph_cell_lists(const Work& w, int l, uint32_t solver = 1) {
     __shared__ uint32_t wr[32], wb[32];
     for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
         const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
-        if (sp->solver != 1) continue;
+        if (sp->solver != solver) continue;
         const MgLevel L = sp->lev[l];
         const uint32_t chunk = item - w.base[si];
         const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
@@ -1004,6 +1004,54 @@ __global__ void __launch_bounds__(1024, 1) k_mg_tail(const SimDev* sims, int n_s
     dep_wait();
 }
 __global__ void __launch_bounds__(THREADS) k_compact(PcgWork pw) { ph_compact(pw); }
+
+// ---------------------------------------------------------------- reference red-black GS
+// Level-0 lists of the simulations that use the reference red-black Gauss-Seidel solve.
+__global__ void __launch_bounds__(THREADS) k_gs_lists(Work w) { ph_cell_lists(w, 0, 0); }
+
+// One colour of one red-black iteration (shaders/fluid.slang:167-182) over the colour's system
+// cells of each chunk, the cells the reference updates (fluid, at least one non-solid
+// neighbour): p = (sum of fluid neighbours' p in the order -x +x -y +y -z +z - div h h / dt) / cnt.
+// A cell reads only the other colour, so visiting the list instead of the grid changes no bit.
+// Before dep_wait() only what stays fixed during the solve is read (lists, records, divergence).
+__global__ void __launch_bounds__(THREADS) k_pressure_rb_list(Work w, uint32_t parity, uint32_t it) {
+    for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
+        const uint32_t item = work_item(w, w_k);
+        const int si = find_sim(w, item);
+        const SimDev* sp = w.sims + si;
+        if (sp->solver != 0 || it >= sp->iterations) continue;
+        const uint32_t chunk = item - w.base[si];
+        const MgLevel& L = sp->lev[0];
+        uint32_t lo, hi;
+        seg(L, chunk, int(parity), lo, hi);
+        const uint32_t* __restrict__ lst = list_of(L, chunk);
+        const uint32_t e0 = lo + threadIdx.x;
+        const bool h0 = e0 < hi;
+        const uint32_t c0 = h0 ? __ldcg(lst + e0) : 0u;
+        const uint32_t i0 = h0 ? uint32_t(sp->info[c0]) : 0u;
+        const float rhs_h = sp->h, rhs_dt = sp->dt;
+        const float d0 = h0 ? sp->div[c0] : 0.0f;
+        const uint32_t nx = uint32_t(sp->nx), nxy = nx * uint32_t(sp->ny);
+        float* __restrict__ p = sp->pressure;
+        dep_wait();
+        auto cell = [&](uint32_t c, uint32_t inf, float dv) {
+            float sum = 0.0f;
+            if (inf & 1u) sum += p[c - 1];
+            if (inf & 2u) sum += p[c + 1];
+            if (inf & 4u) sum += p[c - nx];
+            if (inf & 8u) sum += p[c + nx];
+            if (inf & 16u) sum += p[c - nxy];
+            if (inf & 32u) sum += p[c + nxy];
+            p[c] = (sum - dv * rhs_h * rhs_h / rhs_dt) / float((inf >> 8) & 7u);
+        };
+        if (h0) cell(c0, i0, d0);
+        for (uint32_t e = e0 + blockDim.x; e < hi; e += blockDim.x) {
+            const uint32_t c = lst[e];
+            cell(c, sp->info[c], sp->div[c]);
+        }
+    }
+    dep_wait();
+}
 __global__ void __launch_bounds__(THREADS) k_jacobi(Work w) { ph_jacobi(w); dep_wait(); }
 __global__ void __launch_bounds__(THREADS) k_pcg_init(Work w) { ph_init(w); }
 __global__ void __launch_bounds__(THREADS) k_pcg_widen(Work w) { ph_widen(w); dep_wait(); }
@@ -1153,7 +1201,14 @@ static inline Work mkw(const StageWork& sw) { return sw; }
 // known only on the device) at most 8 blocks per SM, block-strided over the list.
 static unsigned grid_w(const StageWork& w) {
     if (!w.act) return grid_of(w.total);
-    const uint32_t cap = uint32_t(sm_count()) * 8u;
+    // PXF_CG_BLOCKS_PER_SM: blocks per SM of a compacted stage (default 8); a stage with at most
+    // that many items gets one block per item.
+    static const uint32_t per_sm = [] {
+        const char* v = std::getenv("PXF_CG_BLOCKS_PER_SM");
+        const int k = v ? std::atoi(v) : 8;
+        return uint32_t(k > 0 ? k : 8);
+    }();
+    const uint32_t cap = uint32_t(sm_count()) * per_sm;
     return w.total < cap ? (w.total ? w.total : 1u) : cap;
 }
 
@@ -1304,6 +1359,16 @@ cudaError_t launch_barrier_selftest(GridBar* bar, int blocks, int skip, long lon
     e = cudaLaunchKernelEx(&cfg, k_barrier_selftest, bar, skip, limit, rounds);
     note_launch("k_barrier_selftest", st);
     return e;
+}
+
+cudaError_t launch_gs_lists(const StageWork& chunks, cudaStream_t st) {
+    k_gs_lists<<<grid_of(chunks.total), THREADS, 0, st>>>(mkw(chunks)); note_launch("k_gs_lists", st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure_rb_list(const StageWork& chunks, uint32_t parity, uint32_t it, cudaStream_t st) {
+    launch_dep("k_pressure_rb", k_pressure_rb_list, grid_of(chunks.total), THREADS, 0, st, mkw(chunks), parity, it);
+    return cudaGetLastError();
 }
 
 // Blocks of the persistent solve that are guaranteed co-resident on this device.

@@ -87,6 +87,9 @@ constexpr long long kBarrierCycles = 4000000000LL;   // about 2 s at the GB300's
 // One cooperative launch that runs the whole precision solve of a substep.
 int pcg_solve_grid(size_t smem);
 constexpr int kActCounters = 1 + 2 * kMaxLevelsK;
+// Reference red-black GS over level-0 system-cell lists (lists first, then one launch per colour).
+cudaError_t launch_gs_lists(const StageWork& chunks, cudaStream_t st);
+cudaError_t launch_pressure_rb_list(const StageWork& chunks, uint32_t parity, uint32_t it, cudaStream_t st);
 cudaError_t launch_barrier_selftest(GridBar* bar, int blocks, int skip, long long limit_cycles, int rounds,
                                     cudaStream_t st);
 cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st);
