@@ -87,6 +87,7 @@ typedef struct {
     int32_t p2g_tile;              /* P2G tile shape index (-1: tuned / default) */
     uint32_t pcg_precond;          /* 0: multigrid V-cycle (default), 1: Jacobi */
     uint32_t mg_coarse_iters;      /* red-black iterations on the coarsest multigrid level, default 2 */
+    uint32_t mg_smooth_pairs;      /* red-black pairs of pre- and of post-smoothing per level, default 2 */
 } pxf_options;
 
 PXF_API void pxf_fluid_desc_init(pxf_fluid_desc* desc);

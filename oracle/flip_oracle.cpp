@@ -67,6 +67,7 @@ template <class T> struct Sim {
     // 3 = as 1 with a multigrid V-cycle preconditioner in FP32 (the CUDA precision solver).
     int pmode = 0;
     uint32_t mg_coarse_iters = 2;    // symmetric red-black iterations on the coarsest level
+    uint32_t mg_pairs = 2;           // red-black pairs of pre- and of post-smoothing per level
     double rtol = 1e-6;
     uint32_t max_iter = 2000, restart = 50;
     uint32_t last_iters = 0;
@@ -312,8 +313,9 @@ template <class T> struct Sim {
     // Geometric V-cycle on the cell grid. Level l+1 halves each axis (ceil); a coarse cell is AIR
     // if any child is AIR, else FLUID if any child is FLUID, else SOLID (children outside the
     // fine grid count as SOLID). Each level's operator is the same 7-point system as level 0
-    // built from its own types. Smoothing is red-black Gauss-Seidel (pre: red, black; post:
-    // black, red), restriction sums the children's residuals times 1/2 and prolongation injects
+    // built from its own types. Smoothing is red-black Gauss-Seidel, mg_pairs pairs per side
+    // (pre: red from zero, black, then (red, black) x (mg_pairs - 1); post: the mirror image,
+    // (black, red) x mg_pairs, the first black with the coarse correction), restriction sums the children's residuals times 1/2 and prolongation injects
     // the coarse correction into every child, so restriction = prolongation^T / 2 and the cycle
     // is a symmetric operator. The coarsest level (<= 512 cells) runs mg_coarse_iters
     // (default 2) red-black iterations followed by as many black-red iterations from zero.
@@ -457,11 +459,13 @@ template <class T> struct Sim {
         }
         smooth(L, 0, true);
         smooth(L, 1, false);
+        for (uint32_t x = 1; x < mg_pairs; x++) { smooth(L, 0, false); smooth(L, 1, false); }
         restrict_to(l);
         vcycle(l + 1);
         prolong_from(l);
         smooth(L, 1, false);
         smooth(L, 0, false);
+        for (uint32_t x = 1; x < mg_pairs; x++) { smooth(L, 1, false); smooth(L, 0, false); }
     }
 
     // Jacobi-preconditioned CG as a state machine shared by both PCG forms and mirrored by the
@@ -823,9 +827,11 @@ int orc_sim_set_pressure(void* p, int mode, double rtol, uint32_t max_iter, uint
     return 0;
 }
 
-int orc_sim_set_mg(void* p, uint32_t coarse_iters) {
+int orc_sim_set_mg(void* p, uint32_t coarse_iters, uint32_t pairs) {
     auto* hd = static_cast<Handle*>(p);
-    if (hd->dbl) hd->d->mg_coarse_iters = coarse_iters; else hd->f->mg_coarse_iters = coarse_iters;
+    if (pairs == 0) pairs = 1;
+    if (hd->dbl) { hd->d->mg_coarse_iters = coarse_iters; hd->d->mg_pairs = pairs; }
+    else { hd->f->mg_coarse_iters = coarse_iters; hd->f->mg_pairs = pairs; }
     return 0;
 }
 

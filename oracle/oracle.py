@@ -40,7 +40,7 @@ def load():
     lib.orc_sim_new.restype = C.c_void_p
     lib.orc_sim_free.argtypes = [C.c_void_p]
     lib.orc_sim_set_pressure.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_uint32, C.c_uint32]
-    lib.orc_sim_set_mg.argtypes = [C.c_void_p, C.c_uint32]
+    lib.orc_sim_set_mg.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32]
     lib.orc_sim_pcg_stats.argtypes = [C.c_void_p, u32p, C.POINTER(C.c_double)]
     lib.orc_sim_stage.argtypes = [C.c_void_p, C.c_int]
     lib.orc_sim_step.argtypes = [C.c_void_p, C.c_uint32]
@@ -154,8 +154,8 @@ class OracleSim:
         modes = {"gs": 0, "pcg": 1, "pcg64": 2, "mgpcg": 3}
         self.lib.orc_sim_set_pressure(self.h, modes.get(mode, mode), rtol, max_iter, restart)
 
-    def set_mg(self, coarse_iters):
-        self.lib.orc_sim_set_mg(self.h, coarse_iters)
+    def set_mg(self, coarse_iters=2, pairs=2):
+        self.lib.orc_sim_set_mg(self.h, coarse_iters, pairs)
 
     def pcg_stats(self):
         it = C.c_uint32()

@@ -35,7 +35,8 @@ class Options(C.Structure):
     _fields_ = [("pressure_solver", C.c_uint32), ("pcg_rtol", C.c_double), ("pcg_max_iter", C.c_uint32),
                 ("pcg_restart", C.c_uint32), ("lift_grid_limits", C.c_uint32), ("keep_p2g_sums", C.c_uint32),
                 ("velocity_sigma", C.c_float), ("velocity_seed", C.c_uint32), ("wait_timeout_s", C.c_double),
-                ("p2g_tile", C.c_int32), ("pcg_precond", C.c_uint32), ("mg_coarse_iters", C.c_uint32)]
+                ("p2g_tile", C.c_int32), ("pcg_precond", C.c_uint32), ("mg_coarse_iters", C.c_uint32),
+                ("mg_smooth_pairs", C.c_uint32)]
 
 
 class StageTime(C.Structure):

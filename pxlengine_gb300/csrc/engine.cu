@@ -354,6 +354,7 @@ int BatchImpl::rebuild() {
             if (mg) {
                 pw.any_mg = true;
                 pw.max_levels = std::max(pw.max_levels, d.tail + 1);
+                pw.max_pairs = std::max(pw.max_pairs, int(d.mg_pairs));
                 pw.setup_levels = std::max(pw.setup_levels, d.nlev);
                 size_t bytes = 0;
                 for (int l = d.tail; l < d.nlev; l++) bytes += 4 * size_t(tail_level_floats(d.lev[l].nc));
@@ -1013,6 +1014,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.restart = opts.pcg_restart ? opts.pcg_restart : 50;
     d.precond = opts.pcg_precond;
     d.coarse_iters = opts.mg_coarse_iters ? opts.mg_coarse_iters : 2;
+    d.mg_pairs = opts.mg_smooth_pairs ? opts.mg_smooth_pairs : 2;
 
     cudaError_t e = cudaMalloc(&s->mem, L.total);
     if (e != cudaSuccess) {
@@ -1139,6 +1141,7 @@ void pxf_options_init(pxf_options* o) {
     o->p2g_tile = -1;
     o->pcg_precond = 0;
     o->mg_coarse_iters = 2;
+    o->mg_smooth_pairs = 2;
 }
 
 int pxf_validate(const pxf_fluid_desc* desc, uint32_t index, uint32_t lift, char* msg, size_t cap) {

@@ -111,7 +111,16 @@ __device__ __forceinline__ uint32_t nchunks0(const SimDev& s) { return (s.nc + k
 __device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
     const uint32_t n = nchunks0(s);
     double p = 0;
-    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) p += __ldcg(s.partial + k);
+    // eight loads in flight per thread, added in the same order as a plain strided loop
+    uint32_t k = threadIdx.x;
+    for (; k + 7 * blockDim.x < n; k += 8 * blockDim.x) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) v[u] = __ldcg(s.partial + k + u * blockDim.x);
+#pragma unroll
+        for (int u = 0; u < 8; u++) p += v[u];
+    }
+    for (; k < n; k += blockDim.x) p += __ldcg(s.partial + k);
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) p += __shfl_down_sync(0xffffffffu, p, d);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -301,6 +310,7 @@ __device__ void ph_info(const Work& w, int l) {
 }
 
 // One red-black half sweep of A z = r on level l over the system cells of one colour.
+// Pass p of a simulation's smoothing pairs runs only if p < its mg_pairs.
 // mode 0: z = (r + sum z_n) / cnt; mode 1: the other colour is zero (z = r / cnt);
 // mode 2: as 0 with the coarse correction of level l+1 added to every neighbour on the fly
 // (fused prolongation); mode 3: as 0, then the chunk's partial r.z over all system cells.
@@ -333,13 +343,15 @@ __device__ __forceinline__ float smooth_cell(uint32_t c, uint32_t inf, float rc,
     return sum / cnt_of(inf);
 }
 
-__device__ void ph_smooth(const Work& w, int l, int color, int mode) {
+__device__ void ph_smooth(const Work& w, int l, int color, int mode_in, int pass) {
     __shared__ double sh[32];
     for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
         const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
         const SimDev* sp = w.sims + si;
-        if (sp->solver != 1 || sp->precond != 0) continue;
+        if (sp->solver != 1 || sp->precond != 0 || uint32_t(pass) >= sp->mg_pairs) continue;
+        // the r.z partial comes with the last red sweep of the simulation's post-smoothing
+        const int mode = (mode_in == 3 && uint32_t(pass) + 1 != sp->mg_pairs) ? 0 : mode_in;
         const MgLevel L = sp->lev[l];
         const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
         const uint32_t chunk = item - w.base[si];
@@ -571,9 +583,14 @@ __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
         }
         for (uint32_t c = threadIdx.x; c < lv[T].nc; c += blockDim.x) lv[T].r[c] = __ldcg(sp->lev[T].r + c);
         __syncthreads();
+        const uint32_t pairs = sp->mg_pairs;
         for (int l = T; l + 1 < NL; l++) {
             tail_smooth(lv[l], 0, 1, nullptr);
             tail_smooth(lv[l], 1, 0, nullptr);
+            for (uint32_t x = 1; x < pairs; x++) {
+                tail_smooth(lv[l], 0, 0, nullptr);
+                tail_smooth(lv[l], 1, 0, nullptr);
+            }
             tail_restrict(lv[l], lv[l + 1]);
         }
         {
@@ -587,6 +604,10 @@ __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
         for (int l = NL - 2; l >= T; l--) {
             tail_smooth(lv[l], 1, 2, &lv[l + 1]);
             tail_smooth(lv[l], 0, 0, nullptr);
+            for (uint32_t x = 1; x < pairs; x++) {
+                tail_smooth(lv[l], 1, 0, nullptr);
+                tail_smooth(lv[l], 0, 0, nullptr);
+            }
         }
         {
             const MgLevel g = sp->lev[T];
@@ -996,7 +1017,10 @@ __device__ __forceinline__ bool any_restart(const SimDev* sims, int n_sims) {
 __global__ void __launch_bounds__(THREADS) k_cell_lists(Work w, int l) { ph_cell_lists(w, l); }
 __global__ void __launch_bounds__(THREADS) k_mg_coarsen(Work w, int l) { ph_coarsen(w, l); }
 __global__ void __launch_bounds__(THREADS) k_mg_info(Work w, int l) { ph_info(w, l); }
-__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode) { ph_smooth(w, l, color, mode); dep_wait(); }
+__global__ void __launch_bounds__(THREADS) k_mg_smooth(Work w, int l, int color, int mode, int pass) {
+    ph_smooth(w, l, color, mode, pass);
+    dep_wait();
+}
 __global__ void __launch_bounds__(THREADS) k_mg_restrict(Work w, int l) { ph_restrict(w, l); dep_wait(); }
 __global__ void __launch_bounds__(1024, 1) k_mg_tail(const SimDev* sims, int n_sims) {
     extern __shared__ float tsm[];
@@ -1122,8 +1146,14 @@ __device__ bool solve_precond(const SolveArgs& a, float* tsm) {
     if (pw.any_mg) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
-            ph_smooth(pw.level[l], l, 1, 0);
+            ph_smooth(pw.level[l], l, 1, 0, 0);
             if (!grid_sync(a.bar)) return false;
+            for (int x = 1; x < pw.max_pairs; x++) {
+                ph_smooth(pw.level[l], l, 0, 0, x);
+                if (!grid_sync(a.bar)) return false;
+                ph_smooth(pw.level[l], l, 1, 0, x);
+                if (!grid_sync(a.bar)) return false;
+            }
             ph_restrict(pw.coarse[l], l);
             if (!grid_sync(a.bar)) return false;
         }
@@ -1131,10 +1161,12 @@ __device__ bool solve_precond(const SolveArgs& a, float* tsm) {
         if (!grid_sync(a.bar)) return false;
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
-            ph_smooth(pw.level[l], l, 1, 2);
-            if (!grid_sync(a.bar)) return false;
-            ph_smooth(pw.level[l], l, 0, l == 0 ? 3 : 0);
-            if (!grid_sync(a.bar)) return false;
+            for (int x = 0; x < pw.max_pairs; x++) {
+                ph_smooth(pw.level[l], l, 1, x == 0 ? 2 : 0, x);
+                if (!grid_sync(a.bar)) return false;
+                ph_smooth(pw.level[l], l, 0, l == 0 ? 3 : 0, x);
+                if (!grid_sync(a.bar)) return false;
+            }
         }
     }
     ph_ctl(pw.sims, pw.n_sims, 2);
@@ -1266,14 +1298,22 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
             // (the red half sweep from zero ran in the kernel that produced this level's r)
-            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0);
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0, 0);
+            for (int x = 1; x < pw.max_pairs; x++) {
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 0, 0, x);
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0, x);
+            }
             launch_dep("k_mg_restrict", k_mg_restrict, grid_w(pw.coarse[l]), THREADS, 0, st, mkw(pw.coarse[l]), l);
         }
         launch_dep("k_mg_tail", k_mg_tail, pw.n_sims, 1024, pw.tail_smem, st, pw.sims, pw.n_sims);
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
-            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 2);
-            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 0, l == 0 ? 3 : 0);
+            for (int x = 0; x < pw.max_pairs; x++) {
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1,
+                           x == 0 ? 2 : 0, x);
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 0,
+                           l == 0 ? 3 : 0, x);
+            }
         }
     }
     return ctl(pw, 2, st);

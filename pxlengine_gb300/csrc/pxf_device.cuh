@@ -67,6 +67,7 @@ struct SimDev {
     uint32_t solver;         // 0 red-black GS, 1 precision PCG
     uint32_t precond;        // precision PCG preconditioner: 0 multigrid V-cycle, 1 Jacobi
     uint32_t coarse_iters;   // symmetric red-black iterations on the coarsest level
+    uint32_t mg_pairs;       // red-black pairs of pre- and of post-smoothing per level
     double rtol;
     uint32_t max_iter, restart;
     float4 *posA, *velA, *posB, *velB;

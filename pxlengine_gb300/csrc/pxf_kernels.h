@@ -64,6 +64,7 @@ struct PcgWork {
     uint32_t* act_n = nullptr;        // counters: [0] chunks, [1 + l] level[l], [1 + kMaxLevelsK + l] coarse[l]
     int setup_levels = 0;
     int max_levels = 0;                 // global-memory levels (below the shared-memory tail)
+    int max_pairs = 1;                  // largest smoothing pair count of the batch's multigrid simulations
     bool any_mg = false, any_jacobi = false;
     size_t tail_smem = 0;               // dynamic shared memory of the tail kernel
 };

@@ -94,7 +94,7 @@ class Fluid:
 def make_options(solver: str = "gs", rtol: float = 1e-6, max_iter: int = 2000, restart: int = 50,
                  lift_grid_limits: bool = False, keep_p2g_sums: bool = False, velocity_sigma: float = 0.0,
                  velocity_seed: int = 0, wait_timeout_s: float = 600.0, p2g_tile: int = -1,
-                 precond: str = "mg", coarse_iters: int = 2) -> L.Options:
+                 precond: str = "mg", coarse_iters: int = 2, smooth_pairs: int = 2) -> L.Options:
     o = L.Options()
     L.load().pxf_options_init(C.byref(o))
     o.pressure_solver = {"gs": L.PXF_PRESSURE_RBGS, "pcg": L.PXF_PRESSURE_PCG}[solver]
@@ -109,6 +109,7 @@ def make_options(solver: str = "gs", rtol: float = 1e-6, max_iter: int = 2000, r
     o.p2g_tile = p2g_tile
     o.pcg_precond = {"mg": 0, "jacobi": 1}[precond]
     o.mg_coarse_iters = coarse_iters
+    o.mg_smooth_pairs = smooth_pairs
     return o
 
 
