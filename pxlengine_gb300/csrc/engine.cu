@@ -430,8 +430,14 @@ int BatchImpl::rebuild() {
         pw.chunks.sim_of = pw.chunks_all.sim_of = w_chunks.sim_of;
         if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "item table upload");
     }
-    // compacted item lists of the CG loop's stages
-    if (any_pcg) {
+    // compacted item lists of the CG loop's stages (batches; PXF_CG_COMPACT=1 / 0 forces them on / off)
+    static const int compact_env = [] {
+        const char* v = std::getenv("PXF_CG_COMPACT");
+        return v ? (v[0] == '1' ? 1 : 0) : -1;
+    }();
+    const bool compact = compact_env < 0 ? n > 1 : compact_env == 1;
+    pw.act_n = nullptr;
+    if (any_pcg && compact) {
         size_t need = pw.chunks.total;
         for (int l = 0; l < kMaxLevels; l++) need += pw.level[l].total + pw.coarse[l].total;
         if (need > cap_act) {

@@ -1198,8 +1198,10 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
         ph_cell_lists(pw.setup[l], l + 1);
         SYNC_OR_RETURN();
     }
-    ph_compact(pw);
-    SYNC_OR_RETURN();
+    if (pw.act_n) {
+        ph_compact(pw);
+        SYNC_OR_RETURN();
+    }
     ph_init(pw.chunks);
     SYNC_OR_RETURN();
     ph_ctl(pw.sims, pw.n_sims, 0);
@@ -1283,10 +1285,12 @@ cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
         k_mg_info<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l); note_launch("k_mg_info", st);
         k_cell_lists<<<grid_of(pw.setup[l].total), THREADS, 0, st>>>(mkw(pw.setup[l]), l + 1); note_launch("k_cell_lists", st);
     }
-    cudaError_t e = cudaMemsetAsync(pw.act_n, 0, kActCounters * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-    const unsigned gc = std::min<unsigned>((pw.chunks_all.total + THREADS - 1) / THREADS, unsigned(sm_count()) * 4u);
-    k_compact<<<gc ? gc : 1u, THREADS, 0, st>>>(pw); note_launch("k_compact", st);
+    if (pw.act_n) {
+        cudaError_t e = cudaMemsetAsync(pw.act_n, 0, kActCounters * sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+        const unsigned gc = std::min<unsigned>((pw.chunks_all.total + THREADS - 1) / THREADS, unsigned(sm_count()) * 4u);
+        k_compact<<<gc ? gc : 1u, THREADS, 0, st>>>(pw); note_launch("k_compact", st);
+    }
     return cudaGetLastError();
 }
 
@@ -1422,7 +1426,7 @@ int pcg_solve_grid(size_t smem) {
 cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t guard, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(pw.act_n, 0, kActCounters * sizeof(uint32_t), st)) != cudaSuccess) return e;
+    if (pw.act_n && (e = cudaMemsetAsync(pw.act_n, 0, kActCounters * sizeof(uint32_t), st)) != cudaSuccess) return e;
     SolveArgs a;
     a.pw = pw;
     a.bar = bar;
