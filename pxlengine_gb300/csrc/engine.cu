@@ -464,9 +464,11 @@ int BatchImpl::rebuild() {
     }
     if (pw.any_mg && (e = mg_tail_attr(pw.tail_smem)) != cudaSuccess) return cuda_fail(e, "tail kernel attribute");
     if (any_pcg && !d_bar) {
-        if ((e = cudaMalloc(&d_bar, sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
-        if ((e = cudaMemset(d_bar, 0, sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
+        // [0]: the persistent solve's barrier, [1]: the cooperative smoothing kernels'
+        if ((e = cudaMalloc(&d_bar, 2 * sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
+        if ((e = cudaMemset(d_bar, 0, 2 * sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
     }
+    pw.sweep_bar = (pw.any_mg && d_bar) ? d_bar + 1 : nullptr;
     if (any_pcg) persist_grid = pcg_solve_grid(pw.tail_smem);
     int rc = capture();
     if (rc) return rc;
@@ -709,11 +711,12 @@ int BatchImpl::wait() {
         if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(spins > 4096 ? 500 : 20));
     }
     cudaEventDestroy(ev);
-    if (persistent && d_bar) {
-        GridBar hb;
-        e = cudaMemcpy(&hb, d_bar, sizeof(hb), cudaMemcpyDeviceToHost);
+    if (d_bar && (persistent || pw.sweep_bar)) {
+        GridBar hb[2];
+        e = cudaMemcpy(hb, d_bar, sizeof(hb), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "grid barrier state");
-        if (hb.err) return fail(PXF_ETIMEDOUT, "the persistent pressure solve stopped: a grid barrier wait timed out");
+        if ((persistent && hb[0].err) || (pw.sweep_bar && hb[1].err))
+            return fail(PXF_ETIMEDOUT, "the pressure solve stopped: a grid barrier wait timed out");
     }
     return PXF_OK;
 }

@@ -1224,6 +1224,33 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
     ph_finish(pw.chunks_all);
 }
 
+// ---------------------------------------------------------------- cooperative smoothing
+// One level's pre-smoothing (and the restriction below it) or post-smoothing as one cooperative
+// launch: the half sweeps run as phases separated by the bounded grid barrier, instead of one
+// dependent launch each. Every block reaches every barrier (phases skip items, never return
+// early), so a barrier only times out if the device stalls; then the error flag is set and the
+// blocks return.
+__global__ void __launch_bounds__(THREADS) k_mg_pre(Work lw, Work cw, int l, int pairs, GridBar* bar) {
+    ph_smooth(lw, l, 1, 0, 0);
+    for (int x = 1; x < pairs; x++) {
+        if (!grid_sync(bar)) return;
+        ph_smooth(lw, l, 0, 0, x);
+        if (!grid_sync(bar)) return;
+        ph_smooth(lw, l, 1, 0, x);
+    }
+    if (!grid_sync(bar)) return;
+    ph_restrict(cw, l);
+}
+
+__global__ void __launch_bounds__(THREADS) k_mg_post(Work lw, int l, int pairs, GridBar* bar) {
+    for (int x = 0; x < pairs; x++) {
+        if (x && !grid_sync(bar)) return;
+        ph_smooth(lw, l, 1, x == 0 ? 2 : 0, x);
+        if (!grid_sync(bar)) return;
+        ph_smooth(lw, l, 0, l == 0 ? 3 : 0, x);
+    }
+}
+
 // ============================================================================ launchers
 // One block per work item (chunk): chunks of the air exit at once, and the block scheduler hands
 // the rest to whichever SM frees first.
@@ -1278,6 +1305,10 @@ cudaError_t mg_tail_attr(size_t smem) {
 }
 
 cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
+    if (pw.sweep_bar) {
+        cudaError_t e = cudaMemsetAsync(pw.sweep_bar, 0, sizeof(GridBar), st);
+        if (e != cudaSuccess) return e;
+    }
     k_cell_lists<<<grid_of(pw.chunks_all.total), THREADS, 0, st>>>(mkw(pw.chunks_all), 0); note_launch("k_cell_lists", st);
     for (int l = 0; l + 1 < pw.setup_levels; l++) {
         if (!pw.setup[l].total) continue;
@@ -1294,11 +1325,60 @@ cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Cooperative launch of a smoothing kernel over at most the blocks that fit on the device at once.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_coop(const char* name, void (*k)(KArgs...), uint32_t items, cudaStream_t st, Args... args) {
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int a = 0, b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_mg_pre, THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_mg_post, THREADS, 0);
+        per_sm = std::max(1, std::min(a, b));
+    }
+    const uint32_t cap = uint32_t(per_sm) * uint32_t(sm_count());
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(items < cap ? (items ? items : 1u) : cap);
+    cfg.blockDim = dim3(THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k, KArgs(args)...);
+    note_launch(name, st);
+    return e;
+}
+
+// PXF_MG_COOP=1 selects the cooperative smoothing kernels (read at each capture). They give the
+// same bits; one dependent launch per half sweep is faster on a single large simulation.
+static bool coop_smoothing() {
+    const char* v = std::getenv("PXF_MG_COOP");
+    return v && v[0] == '1';
+}
+
 cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
     if (pw.any_jacobi) {
         launch_dep("k_jacobi", k_jacobi, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     }
-    if (pw.any_mg) {
+    if (pw.any_mg && coop_smoothing() && pw.sweep_bar) {
+        // one cooperative launch per level and side
+        cudaError_t e;
+        for (int l = 0; l + 1 < pw.max_levels; l++) {
+            if (!pw.level[l].total) continue;
+            const uint32_t items = std::max(pw.level[l].total, pw.coarse[l].total);
+            if ((e = launch_coop("k_mg_pre", k_mg_pre, items, st, mkw(pw.level[l]), mkw(pw.coarse[l]), l, pw.max_pairs,
+                                 pw.sweep_bar)) != cudaSuccess)
+                return e;
+        }
+        launch_dep("k_mg_tail", k_mg_tail, pw.n_sims, 1024, pw.tail_smem, st, pw.sims, pw.n_sims);
+        for (int l = pw.max_levels - 2; l >= 0; l--) {
+            if (!pw.level[l].total) continue;
+            if ((e = launch_coop("k_mg_post", k_mg_post, pw.level[l].total, st, mkw(pw.level[l]), l, pw.max_pairs,
+                                 pw.sweep_bar)) != cudaSuccess)
+                return e;
+        }
+    } else if (pw.any_mg) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
             // (the red half sweep from zero ran in the kernel that produced this level's r)

@@ -62,6 +62,7 @@ struct PcgWork {
     StageWork coarse[kMaxLevelsK];    // level-(l+1) chunks of those simulations, compacted
     StageWork setup[kMaxLevelsK];     // level-(l+1) chunks of every multigrid simulation with level l+1
     uint32_t* act_n = nullptr;        // counters: [0] chunks, [1 + l] level[l], [1 + kMaxLevelsK + l] coarse[l]
+    struct GridBar* sweep_bar = nullptr;  // grid barrier of the cooperative smoothing kernels
     int setup_levels = 0;
     int max_levels = 0;                 // global-memory levels (below the shared-memory tail)
     int max_pairs = 1;                  // largest smoothing pair count of the batch's multigrid simulations

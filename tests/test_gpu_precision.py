@@ -73,20 +73,22 @@ def test_pcg_iteration_cap_reports_status(lib):
 
 @pytest.mark.parametrize("precond", ["mg", "jacobi"])
 def test_persistent_solve_matches_graph_loop(lib, monkeypatch, precond):
-    """The persistent cooperative solve (one launch, grid barriers) runs the same phases over the
-    same chunks as the graph of kernels, so both give identical bits."""
+    """The persistent cooperative solve (one launch, grid barriers) and the cooperative smoothing
+    kernels run the same phases over the same chunks as the graph of kernels, so all three give
+    identical bits."""
     f = dam(res=48, ppc=4)
     opts = P.make_options(solver="pcg", rtol=PCG_RTOL, max_iter=4000, restart=50, precond=precond)
     out = {}
-    for mode in ("0", "1"):
-        monkeypatch.setenv("PXF_PCG_PERSISTENT", mode)
+    for mode, env in (("graph", {}), ("persistent", {"PXF_PCG_PERSISTENT": "1"}), ("coop", {"PXF_MG_COOP": "1"})):
+        for k in ("PXF_PCG_PERSISTENT", "PXF_MG_COOP"):
+            monkeypatch.setenv(k, env.get(k, "0"))
         with P.FluidState(f, fps=15.0, options=opts) as s:
             s.step(3)
             out[mode] = (s.read_particles(), s.read_grid("pressure64"), s.solver_stats())
-    assert out["0"][2][2] == 0 and out["1"][2][2] == 0
-    assert out["0"][2][0] == out["1"][2][0]
-    assert np.array_equal(out["0"][0], out["1"][0])
-    assert np.array_equal(out["0"][1], out["1"][1])
+    for mode in ("persistent", "coop"):
+        assert out[mode][2][2] == 0 and out[mode][2][0] == out["graph"][2][0]
+        assert np.array_equal(out[mode][0], out["graph"][0])
+        assert np.array_equal(out[mode][1], out["graph"][1])
 
 
 def test_precision_solve_is_deterministic(lib):
