@@ -366,13 +366,66 @@ __device__ void ph_smooth(const Work& w, int l, int color, int mode_in, int pass
         const bool h0 = e0 < hi;
         const uint32_t c0 = h0 ? __ldcg(lst + e0) : 0u;
         const uint32_t i0 = h0 ? uint32_t(info[c0]) : 0u;
+        // mode 2: the coarse cells above the first cell's neighbours and whether they are in the
+        // coarse system (both fixed during the solve)
+        uint32_t P[6] = {0, 0, 0, 0, 0, 0};
+        uint32_t pin = 0;
+        if (h0 && mode == 2) {
+            const uint32_t i = c0 % nx, j = (c0 / nx) % ny, kk = c0 / nxy;
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                if (!(i0 & (1u << q))) continue;
+                const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                P[q] = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
+                       cnxy * (uint32_t(int(kk) + dz) >> 1);
+                if (in_system(Cc.info[P[q]])) pin |= 1u << q;
+            }
+        }
         dep_wait();
         const float* __restrict__ r = L.r;
         float* __restrict__ z = L.z;
+        // every value the first cell needs, issued together with the convergence flag
         const uint32_t done = ldu(&sp->pcg->done);
-        const float r0 = h0 ? r[c0] : 0.0f;
+        float r0 = 0.0f, zn[6], zc[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            zn[q] = 0.0f;
+            zc[q] = 0.0f;
+        }
+        if (h0) {
+            r0 = r[c0];
+            if (mode != 1) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (i0 & (1u << q)) zn[q] = z[uint32_t(int64_t(c0) + nbr(q, nx, nxy))];
+            }
+            if (mode == 2) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (pin & (1u << q)) zc[q] = Cc.z[P[q]];
+            }
+        }
         if (done) continue;
-        if (h0) z[c0] = smooth_cell(c0, i0, r0, z, mode, nx, ny, nxy, Cc, cnx, cnxy);
+        if (h0) {
+            // the same sums, in the same order, as smooth_cell
+            float sum = r0;
+            if (mode == 2) {
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    if (!(i0 & (1u << q))) continue;
+                    float t = zn[q];
+                    if (pin & (1u << q)) t += zc[q];
+                    sum += t;
+                }
+            } else if (mode != 1) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (i0 & (1u << q)) sum += zn[q];
+            }
+            z[c0] = sum / cnt_of(i0);
+        }
         for (uint32_t e = e0 + blockDim.x; e < hi; e += blockDim.x) {
             const uint32_t c = lst[e];
             z[c] = smooth_cell(c, info[c], r[c], z, mode, nx, ny, nxy, Cc, cnx, cnxy);
@@ -814,17 +867,54 @@ __device__ void ph_dir(const Work& w) {
         const uint32_t pbuf = ldu(&st->pbuf);
         const bool fresh = ldu(&st->fresh) != 0;
         const double betad = ldd(&st->beta);
+        const float* __restrict__ z = s.z;
+        const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
+        // the first two cells' z and p of both direction buffers, issued with the scalars (which
+        // buffer holds the old direction is one of them)
+        float za[2][7], pa[2][7], pb[2][7];
+        const uint32_t cc[2] = {t.c0, t.c1}, ii[2] = {t.i0, t.i1};
+        const bool hh[2] = {t.h0, t.h1};
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+#pragma unroll
+            for (int q = 0; q < 7; q++) {
+                za[u][q] = 0.f;
+                pa[u][q] = 0.f;
+                pb[u][q] = 0.f;
+            }
+            if (!hh[u]) continue;
+            za[u][6] = z[cc[u]];
+            pa[u][6] = s.p0[cc[u]];
+            pb[u][6] = s.p1[cc[u]];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {
+                if (!(ii[u] & (1u << q))) continue;
+                const int64_t n = int64_t(cc[u]) + nbr(q, nx, nxy);
+                za[u][q] = z[n];
+                pa[u][q] = s.p0[n];
+                pb[u][q] = s.p1[n];
+            }
+        }
         if (done) continue;
         const float beta = fresh ? 0.0f : float(betad);
         const float* __restrict__ pold = pbuf ? s.p1 : s.p0;
         float* __restrict__ pnew = pbuf ? s.p0 : s.p1;
-        const float* __restrict__ z = s.z;
         float* __restrict__ Ap = s.Ap;
-        const int64_t nx = s.nx, nxy = int64_t(s.nx) * s.ny;
         DF acc{0.f, 0.f};
-        DirCell d0{0.f, 0.f}, d1{0.f, 0.f};
-        if (t.h0) d0 = dir_cell(t.c0, t.i0, z, pold, fresh, beta, nx, nxy);
-        if (t.h1) d1 = dir_cell(t.c1, t.i1, z, pold, fresh, beta, nx, nxy);
+        DirCell dd[2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (!hh[u]) continue;
+            // dir_cell's arithmetic on the values loaded above
+            const float* po = pbuf ? pb[u] : pa[u];
+            const float pn = fresh ? za[u][6] : za[u][6] + beta * po[6];
+            float ap = cnt_of(ii[u]) * pn;
+#pragma unroll
+            for (int q = 0; q < 6; q++)
+                if (ii[u] & (1u << q)) ap -= fresh ? za[u][q] : za[u][q] + beta * po[q];
+            dd[u] = {pn, ap};
+        }
+        const DirCell d0 = dd[0], d1 = dd[1];
         if (t.h0) {
             pnew[t.c0] = d0.pn;
             Ap[t.c0] = d0.ap;
@@ -877,9 +967,12 @@ __device__ void ph_update(const Work& w) {
         float r0 = 0.f, r1 = 0.f, a0 = 0.f, a1 = 0.f;
         if (t.h0) { x0 = x2[t.c0]; r0 = r[t.c0]; a0 = Ap[t.c0]; }
         if (t.h1) { x1 = x2[t.c1]; r1 = r[t.c1]; a1 = Ap[t.c1]; }
+        // p of both direction buffers (which one is current is among the scalars above)
+        const float q00 = t.h0 ? s.p0[t.c0] : 0.f, q01 = t.h0 ? s.p1[t.c0] : 0.f;
+        const float q10 = t.h1 ? s.p0[t.c1] : 0.f, q11 = t.h1 ? s.p1[t.c1] : 0.f;
         if (done) continue;
         const float* __restrict__ p = pbuf ? s.p1 : s.p0;
-        const float p0v = t.h0 ? p[t.c0] : 0.f, p1v = t.h1 ? p[t.c1] : 0.f;
+        const float p0v = pbuf ? q01 : q00, p1v = pbuf ? q11 : q10;
         DF acc{0.f, 0.f};
         auto one = [&](uint32_t e, uint32_t c, uint32_t inf, float pc, float2 x, float rc, float apc) {
             DF d = two_prod(ah, pc);
