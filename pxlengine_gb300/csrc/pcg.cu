@@ -1318,29 +1318,178 @@ __global__ void __launch_bounds__(THREADS) k_pcg_solve(SolveArgs a) {
 }
 
 // ---------------------------------------------------------------- cooperative smoothing
-// One level's pre-smoothing (and the restriction below it) or post-smoothing as one cooperative
-// launch: the half sweeps run as phases separated by the bounded grid barrier, instead of one
-// dependent launch each. Every block reaches every barrier (phases skip items, never return
-// early), so a barrier only times out if the device stalls; then the error flag is set and the
-// blocks return.
-__global__ void __launch_bounds__(THREADS) k_mg_pre(Work lw, Work cw, int l, int pairs, GridBar* bar) {
-    ph_smooth(lw, l, 1, 0, 0);
-    for (int x = 1; x < pairs; x++) {
-        if (!grid_sync(bar)) return;
-        ph_smooth(lw, l, 0, 0, x);
-        if (!grid_sync(bar)) return;
-        ph_smooth(lw, l, 1, 0, x);
+// One level's pre-smoothing (with the restriction below it) or post-smoothing as one cooperative
+// launch: its half sweeps run as phases separated by the bounded grid barrier instead of one
+// dependent launch each. Block b owns the level's chunks b, b + grid, ... (at most kCoopCPB);
+// their cell lists and neighbour records, fixed during the solve, are read into shared memory once
+// and every sweep then reads only r and z. In each round a thread takes one list entry of each of
+// its block's chunks and issues all their loads before any store. Every block reaches every
+// barrier (phases skip work, never return early); a barrier that times out sets the error flag and
+// the blocks return.
+constexpr int kCoopCPB = 4;
+
+struct CoopChunk {
+    uint32_t si, chunk, nred, nsys;   // nsys = 0: nothing to smooth (no chunk, other solver, done)
+};
+
+__device__ __forceinline__ void coop_sweep(const Work& lw, int l, int color, int mode_in, int pass, const CoopChunk* ch,
+                                           const uint32_t* cells, const uint16_t* infos, uint32_t cs, double* sh) {
+    constexpr int J = kCoopCPB;
+    // per chunk: effective mode (-1: skip) and colour segment
+    int mode[J];
+    uint32_t lo[J], hi[J];
+    uint32_t rounds = 0;
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        mode[j] = -1;
+        lo[j] = hi[j] = 0;
+        if (!ch[j].nsys) continue;
+        const SimDev* sp = lw.sims + ch[j].si;
+        if (uint32_t(pass) >= sp->mg_pairs) continue;
+        mode[j] = (mode_in == 3 && uint32_t(pass) + 1 != sp->mg_pairs) ? 0 : mode_in;
+        lo[j] = color == 1 ? ch[j].nred : 0u;
+        hi[j] = color == 0 ? ch[j].nred : ch[j].nsys;
+        rounds = max(rounds, (hi[j] - lo[j] + blockDim.x - 1) / blockDim.x);
     }
-    if (!grid_sync(bar)) return;
-    ph_restrict(cw, l);
+    for (uint32_t rr = 0; rr < rounds; rr++) {
+        float rv[J], zn[J][6], zc[J][6];
+        uint32_t cc[J], ii[J], pin[J];
+        uint32_t P[J][6];
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const uint32_t e = lo[j] + threadIdx.x + rr * blockDim.x;
+            const bool h = mode[j] >= 0 && e < hi[j];
+            cc[j] = h ? cells[j * cs + e] : 0u;
+            ii[j] = h ? uint32_t(infos[j * cs + e]) : 0u;   // zero record: nothing to do
+            pin[j] = 0;
+            rv[j] = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 6; q++) { zn[j][q] = 0.0f; zc[j][q] = 0.0f; P[j][q] = 0u; }
+            if (!h) continue;
+            const SimDev* sp = lw.sims + ch[j].si;
+            const MgLevel& L = sp->lev[l];
+            const uint32_t nx = uint32_t(L.nx), ny = uint32_t(L.ny), nxy = nx * ny;
+            rv[j] = L.r[cc[j]];
+            if (mode[j] != 1) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (ii[j] & (1u << q)) zn[j][q] = L.z[uint32_t(int64_t(cc[j]) + nbr(q, nx, nxy))];
+            }
+            if (mode[j] == 2) {
+                const MgLevel& Cc = sp->lev[l + 1];
+                const uint32_t cnx = uint32_t(Cc.nx), cnxy = uint32_t(Cc.nx) * uint32_t(Cc.ny);
+                const uint32_t c = cc[j], i = c % nx, jj = (c / nx) % ny, kk = c / nxy;
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    if (!(ii[j] & (1u << q))) continue;
+                    const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                    const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                    const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                    P[j][q] = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(jj) + dy) >> 1) +
+                              cnxy * (uint32_t(int(kk) + dz) >> 1);
+                    if (in_system(Cc.info[P[j][q]])) {
+                        pin[j] |= 1u << q;
+                        zc[j][q] = Cc.z[P[j][q]];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            if (!ii[j]) continue;
+            // smooth_cell's sums, in its order
+            float sum = rv[j];
+            if (mode[j] == 2) {
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    if (!(ii[j] & (1u << q))) continue;
+                    float t = zn[j][q];
+                    if (pin[j] & (1u << q)) t += zc[j][q];
+                    sum += t;
+                }
+            } else if (mode[j] != 1) {
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (ii[j] & (1u << q)) sum += zn[j][q];
+            }
+            lw.sims[ch[j].si].lev[l].z[cc[j]] = sum / cnt_of(ii[j]);
+        }
+    }
+    // r.z partials of the chunks whose last post-smoothing sweep this was (block-uniform)
+    bool any3 = false;
+#pragma unroll
+    for (int j = 0; j < J; j++) any3 |= mode[j] == 3;
+    if (any3) {
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            if (mode[j] != 3) continue;
+            const SimDev* sp = lw.sims + ch[j].si;
+            const MgLevel& L = sp->lev[l];
+            DF acc{0.f, 0.f};
+            for (uint32_t e = threadIdx.x; e < ch[j].nsys; e += blockDim.x) {
+                const uint32_t c = cells[j * cs + e];
+                acc = df_add(acc, two_prod(L.r[c], L.z[c]));
+            }
+            const double t = block_sum(acc, sh);
+            if (threadIdx.x == 0) sp->partial[ch[j].chunk] = t;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(THREADS) k_mg_post(Work lw, int l, int pairs, GridBar* bar) {
-    for (int x = 0; x < pairs; x++) {
-        if (x && !grid_sync(bar)) return;
-        ph_smooth(lw, l, 1, x == 0 ? 2 : 0, x);
+// side 0: pre-smoothing and the restriction to level l+1; side 1: post-smoothing.
+__global__ void __launch_bounds__(THREADS, 4) k_mg_level(Work lw, Work cw, int l, int side, int pairs, uint32_t cs,
+                                                      GridBar* bar) {
+    extern __shared__ uint32_t coop_mem[];
+    __shared__ CoopChunk ch[kCoopCPB];
+    __shared__ double sh[32];
+    uint32_t* cells = coop_mem;
+    uint16_t* infos = reinterpret_cast<uint16_t*>(coop_mem + kCoopCPB * cs);
+    if (threadIdx.x < kCoopCPB) {
+        CoopChunk c{0u, 0u, 0u, 0u};
+        const uint32_t k = blockIdx.x + threadIdx.x * gridDim.x;
+        if (k < lw.total) {
+            const int si = find_sim(lw, k);
+            const SimDev* sp = lw.sims + si;
+            if (sp->solver == 1 && sp->precond == 0 && !ldu(&sp->pcg->done)) {
+                const MgLevel& L = sp->lev[l];
+                c.si = uint32_t(si);
+                c.chunk = k - lw.base[si];
+                c.nred = __ldcg(L.lcnt + 2 * c.chunk);
+                c.nsys = c.nred + __ldcg(L.lcnt + 2 * c.chunk + 1);
+            }
+        }
+        ch[threadIdx.x] = c;
+    }
+    __syncthreads();
+    for (int j = 0; j < kCoopCPB; j++) {
+        if (!ch[j].nsys) continue;
+        const MgLevel& L = lw.sims[ch[j].si].lev[l];
+        const uint32_t* lst = list_of(L, ch[j].chunk);
+        for (uint32_t e = threadIdx.x; e < ch[j].nsys; e += blockDim.x) {
+            const uint32_t c = __ldcg(lst + e);
+            cells[j * cs + e] = c;
+            infos[j * cs + e] = L.info[c];
+        }
+    }
+    __syncthreads();
+    if (side == 0) {
+        coop_sweep(lw, l, 1, 0, 0, ch, cells, infos, cs, sh);
+        for (int x = 1; x < pairs; x++) {
+            if (!grid_sync(bar)) return;
+            coop_sweep(lw, l, 0, 0, x, ch, cells, infos, cs, sh);
+            if (!grid_sync(bar)) return;
+            coop_sweep(lw, l, 1, 0, x, ch, cells, infos, cs, sh);
+        }
         if (!grid_sync(bar)) return;
-        ph_smooth(lw, l, 0, l == 0 ? 3 : 0, x);
+        ph_restrict(cw, l);
+    } else {
+        for (int x = 0; x < pairs; x++) {
+            if (x && !grid_sync(bar)) return;
+            coop_sweep(lw, l, 1, x == 0 ? 2 : 0, x, ch, cells, infos, cs, sh);
+            if (!grid_sync(bar)) return;
+            coop_sweep(lw, l, 0, l == 0 ? 3 : 0, x, ch, cells, infos, cs, sh);
+        }
     }
 }
 
@@ -1418,33 +1567,43 @@ cudaError_t launch_mg_setup(const PcgWork& pw, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// Cooperative launch of a smoothing kernel over at most the blocks that fit on the device at once.
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_coop(const char* name, void (*k)(KArgs...), uint32_t items, cudaStream_t st, Args... args) {
-    static int per_sm = -1;
-    if (per_sm < 0) {
-        int a = 0, b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_mg_pre, THREADS, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_mg_post, THREADS, 0);
-        per_sm = std::max(1, std::min(a, b));
-    }
-    const uint32_t cap = uint32_t(per_sm) * uint32_t(sm_count());
+// Cooperative launch of k_mg_level over `grid` blocks with `smem` bytes of cached lists.
+static cudaError_t launch_coop(unsigned grid, size_t smem, cudaStream_t st, const Work& lw, const Work& cw, int l,
+                               int side, int pairs, uint32_t cs, GridBar* bar) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(items < cap ? (items ? items : 1u) : cap);
+    cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, k, KArgs(args)...);
-    note_launch(name, st);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_mg_level, lw, cw, l, side, pairs, cs, bar);
+    note_launch(side == 0 ? "k_mg_pre" : "k_mg_post", st);
     return e;
 }
 
-// PXF_MG_COOP=1 selects the cooperative smoothing kernels (read at each capture). They give the
-// same bits; one dependent launch per half sweep is faster on a single large simulation.
+// Grid of the cooperative smoothing of a level: enough blocks that each caches at most kCoopCPB
+// chunks, all co-resident; 0 when the level does not fit (it then runs one launch per sweep).
+static unsigned coop_grid(const StageWork& lw, uint32_t cs, size_t* smem) {
+    if (lw.act) return 0;
+    *smem = size_t(kCoopCPB) * cs * 6;
+    if (*smem > 200 * 1024) return 0;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_mg_level, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_level, THREADS, *smem) != cudaSuccess) return 0;
+    const uint32_t cap = uint32_t(per_sm) * uint32_t(sm_count());
+    const uint32_t need = (lw.total + kCoopCPB - 1) / kCoopCPB;
+    if (need > cap || cap == 0) return 0;
+    return std::min<uint32_t>(cap, std::max<uint32_t>(need, std::min<uint32_t>(lw.total, cap)));
+}
+
 static bool coop_smoothing() {
     const char* v = std::getenv("PXF_MG_COOP");
     return v && v[0] == '1';
@@ -1455,21 +1614,44 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
         launch_dep("k_jacobi", k_jacobi, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     }
     if (pw.any_mg && coop_smoothing() && pw.sweep_bar) {
-        // one cooperative launch per level and side
+        // one cooperative launch per level and side where the level fits, else one launch per sweep
         cudaError_t e;
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
-            const uint32_t items = std::max(pw.level[l].total, pw.coarse[l].total);
-            if ((e = launch_coop("k_mg_pre", k_mg_pre, items, st, mkw(pw.level[l]), mkw(pw.coarse[l]), l, pw.max_pairs,
-                                 pw.sweep_bar)) != cudaSuccess)
-                return e;
+            const uint32_t cs = l == 0 ? kScanChunk : kCoarseChunk;
+            size_t smem = 0;
+            const unsigned g = coop_grid(pw.level[l], cs, &smem);
+            if (g) {
+                if ((e = launch_coop(g, smem, st, mkw(pw.level[l]), mkw(pw.coarse[l]), l, 0, pw.max_pairs, cs,
+                                     pw.sweep_bar)) != cudaSuccess)
+                    return e;
+                continue;
+            }
+            launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0, 0);
+            for (int x = 1; x < pw.max_pairs; x++) {
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 0, 0, x);
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1, 0, x);
+            }
+            launch_dep("k_mg_restrict", k_mg_restrict, grid_w(pw.coarse[l]), THREADS, 0, st, mkw(pw.coarse[l]), l);
         }
         launch_dep("k_mg_tail", k_mg_tail, pw.n_sims, 1024, pw.tail_smem, st, pw.sims, pw.n_sims);
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
-            if ((e = launch_coop("k_mg_post", k_mg_post, pw.level[l].total, st, mkw(pw.level[l]), l, pw.max_pairs,
-                                 pw.sweep_bar)) != cudaSuccess)
-                return e;
+            const uint32_t cs = l == 0 ? kScanChunk : kCoarseChunk;
+            size_t smem = 0;
+            const unsigned g = coop_grid(pw.level[l], cs, &smem);
+            if (g) {
+                if ((e = launch_coop(g, smem, st, mkw(pw.level[l]), mkw(pw.level[l]), l, 1, pw.max_pairs, cs,
+                                     pw.sweep_bar)) != cudaSuccess)
+                    return e;
+                continue;
+            }
+            for (int x = 0; x < pw.max_pairs; x++) {
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 1,
+                           x == 0 ? 2 : 0, x);
+                launch_dep("k_mg_smooth", k_mg_smooth, grid_w(pw.level[l]), THREADS, 0, st, mkw(pw.level[l]), l, 0,
+                           l == 0 ? 3 : 0, x);
+            }
         }
     } else if (pw.any_mg) {
         for (int l = 0; l + 1 < pw.max_levels; l++) {
