@@ -126,10 +126,10 @@ class ClockSampler:
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from
 # one ncu capture of this workload, keyed by (config, kernel); the capture is summarised in profiles/.
 KERNEL_TRAFFIC = {
-    ("dam256", "k_p2g"): 432.19e6,
-    ("dam256", "k_g2p"): 543.56e6,
-    ("dam256", "k_pcg_update"): 28.78e6,
-    ("dam256_gs", "k_pressure_rb"): 16.70e6,
+    ("dam256", "k_p2g"): 432.20e6,
+    ("dam256", "k_g2p"): 543.13e6,
+    ("dam256", "k_pcg_update"): 33.61e6,
+    ("dam256_gs", "k_pressure_rb_list"): 12.48e6,
 }
 
 
@@ -168,6 +168,7 @@ def kernel_bytes(kernel, N, F, C, Cf, lv=None):
         "k_p2g": 32 * N + 8 * F + 4 * C,             # sorted particles and cell starts in; vel, vel_old out
         "k_divergence": 4 * F + 1 * C + 4 * C + 2 * C,   # faces, flags in; divergence, neighbour record out
         "k_pressure_rb": 8 * C,                      # one colour: 16C per red-black iteration
+        "k_pressure_rb_list": 8 * C,                 # the same sweep over the system-cell lists
         "k_pcg_dir": 22 * Cf,                        # list, z, p, record in; p', Ap out
         "k_pcg_update": 38 * Cf,                     # list, p, Ap, r, x (8 B) in; r, x, red z out
         "k_project": 8 * F + 5 * C,                  # faces in and out; pressure, flags in

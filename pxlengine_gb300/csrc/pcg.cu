@@ -1766,7 +1766,7 @@ cudaError_t launch_gs_lists(const StageWork& chunks, cudaStream_t st) {
 }
 
 cudaError_t launch_pressure_rb_list(const StageWork& chunks, uint32_t parity, uint32_t it, cudaStream_t st) {
-    launch_dep("k_pressure_rb", k_pressure_rb_list, grid_of(chunks.total), THREADS, 0, st, mkw(chunks), parity, it);
+    launch_dep("k_pressure_rb_list", k_pressure_rb_list, grid_of(chunks.total), THREADS, 0, st, mkw(chunks), parity, it);
     return cudaGetLastError();
 }
 
