@@ -246,6 +246,26 @@ def divergence_linf(sim):
     return float(np.max(np.abs(d[fl])) * sim.dt) if fl.any() else 0.0
 
 
+def fp64_check(sim, cfg):
+    """One more substep of the GPU simulation against the oracle's FP64 solve of the same pressure
+    system (the oracle's pre-pressure stages are bit-exact with the GPU's): max pressure error
+    relative to max |p64|, and max |div v| * dt after the GPU's projection."""
+    import numpy as np
+    import oracle
+    p0 = sim.read_particles()
+    o = oracle.OracleSim(sim.dims, sim.cell, sim.dt, 0.95, list(cfg["bounds"][0]), [0, -9.81, 0], cfg["iterations"],
+                         p0)
+    o.set_pressure("pcg64", rtol=1e-10, max_iter=100000)
+    sim.step(1)
+    for st in ("clear", "p2g", "normalize", "forces", "divergence", "pressure"):
+        o.stage(st)
+    p64 = o.read(oracle.PRESSURE64)
+    pg = sim.read_grid("pressure64")
+    scale = max(1e-30, float(np.max(np.abs(p64))))
+    return {"pressure_rel_err_vs_fp64": float(np.max(np.abs(pg - p64))) / scale,
+            "divergence_linf_dt": divergence_linf(sim), "fp64_rtol": 1e-10}
+
+
 def pct(xs, q):
     import numpy as np
     return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else None
@@ -360,6 +380,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--fp64-check", action="store_true",
+                    help="after the run, compare one substep's pressure with the oracle's FP64 solve")
     args = ap.parse_args()
     cfg = CONFIGS.get(args.config)
     rank = env_int("RANK", 0)
@@ -542,6 +564,12 @@ def main():
                    "triangles": int(m["indices"].shape[0]), "overflow": m["overflow"],
                    "surface_cells": list(info["dims"])}
 
+    precision = None
+    if cfg["solver"] == "pcg" and rank == 0:
+        precision = {"divergence_linf_dt": divergence_linf(sim)}
+        if args.fp64_check:
+            precision = fp64_check(sim, cfg)
+
     launches_per_substep = sum(k["launches"] for k in kernels) if kernels else None
     solver_stats = None
     if cfg["solver"] == "pcg":
@@ -562,7 +590,8 @@ def main():
                 "substep_roofline": substep_roofline,
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": (launches_per_substep * args.steps) if launches_per_substep else None,
-                "solver": solver_stats, "kernels": kernels, "surface_mesh": surface, "wall_s_timed": t_wall}
+                "solver": solver_stats, "precision": precision, "kernels": kernels, "surface_mesh": surface,
+                "wall_s_timed": t_wall}
         print(json.dumps(line), flush=True)
     sim.close()
     if dist:
