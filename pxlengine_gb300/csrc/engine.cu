@@ -279,6 +279,7 @@ int BatchImpl::rebuild() {
     }
     drop_graphs();
     const int n = int(sims.size());
+    trace("rebuild: %d simulations", n);
     if (n == 0) { dirty = false; return PXF_OK; }
     if (n > 65535) return fail(PXF_EINVAL, "a batch holds at most 65535 simulations");
     if (size_t(n) > cap_sims) {
@@ -301,9 +302,6 @@ int BatchImpl::rebuild() {
     // P2G tile indexes of every shape (the autotuner times them all)
     if (size_t(n) + 1 > cap_tile) {
         if (d_tile_base) cudaFree(d_tile_base);
-    if (d_sim_of) cudaFree(d_sim_of);
-    if (d_act) cudaFree(d_act);
-    if (d_act_n) cudaFree(d_act_n);
         d_tile_base = nullptr;
         cap_tile = std::max<size_t>(size_t(n) + 1, 2 * cap_tile);
         if ((e = cudaMalloc(&d_tile_base, kNumP2GShapes * cap_tile * sizeof(uint32_t))) != cudaSuccess)
@@ -470,7 +468,9 @@ int BatchImpl::rebuild() {
     }
     pw.sweep_bar = (pw.any_mg && d_bar) ? d_bar + 1 : nullptr;
     if (any_pcg) persist_grid = pcg_solve_grid(pw.tail_smem);
+    trace("rebuild: indexes uploaded, capturing");
     int rc = capture();
+    trace("rebuild: capture rc=%d", rc);
     if (rc) return rc;
     dirty = false;
     return PXF_OK;
@@ -909,6 +909,22 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
 }
 
 void set_global_error_message(const std::string& m) { g_last_error = m; }
+
+bool trace_on() {
+    static const bool on = [] { const char* v = std::getenv("PXF_TRACE"); return v && v[0] == '1'; }();
+    return on;
+}
+
+void trace(const char* fmt, ...) {
+    if (!trace_on()) return;
+    va_list ap;
+    va_start(ap, fmt);
+    std::fprintf(stderr, "[pxf] ");
+    std::vfprintf(stderr, fmt, ap);
+    std::fprintf(stderr, "\n");
+    std::fflush(stderr);
+    va_end(ap);
+}
 
 int p2g_lanes_default() {
     static const int lanes = [] { const char* v = std::getenv("PXF_P2G_STRIDED"); return v ? (std::atoi(v) ? 1 : 0) : 1; }();

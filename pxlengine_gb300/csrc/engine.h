@@ -7,4 +7,8 @@ namespace pxf {
 int p2g_shape_index();
 int p2g_lanes_default();
 
+// PXF_TRACE=1: one line per library step on stderr (flushed), for locating host-side failures.
+bool trace_on();
+void trace(const char* fmt, ...);
+
 }  // namespace pxf

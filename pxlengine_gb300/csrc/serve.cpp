@@ -26,6 +26,7 @@
 #include <thread>
 #include <vector>
 
+#include "engine.h"
 #include "../../include/pxlflip.h"
 #include "scene.h"
 
@@ -91,6 +92,7 @@ namespace {
 // Moves a finished or cancelled request's particles to the host and frees its device state.
 void release(pxf_server* S, Request* r, bool keep_result) {
     if (!r->sim) return;
+    pxf::trace("serve: release request %llu", (unsigned long long)r->id);
     pxf_batch_remove(S->batch, r->sim);
     if (keep_result) {
         r->result.resize(size_t(r->particles) * 8);
@@ -142,7 +144,9 @@ int tick_impl(pxf_server* S, uint32_t* active_out) {
             pxf_fluid_desc d;
             r->cfg.to_desc(d);
             pxf_sim* sim = nullptr;
+            pxf::trace("serve: admit request %llu", (unsigned long long)r->id);
             int rc = pxf_create_ex(&d, r->seed, r->fps, &r->opts, &sim);
+            pxf::trace("serve: created rc=%d", rc);
             if (rc == PXF_OK) rc = pxf_batch_add(S->batch, sim);
             if (rc != PXF_OK) {
                 r->state = PXF_REQ_FAILED;
@@ -171,7 +175,9 @@ int tick_impl(pxf_server* S, uint32_t* active_out) {
         uint32_t need = n;
         for (Request* r : step_set) need = std::min(need, r->total - r->done);
         if (need == 0) need = 1;
+        pxf::trace("serve: step %zu requests", step_set.size());
         rc = pxf_batch_step_timed(S->batch, need, &ms);
+        pxf::trace("serve: step rc=%d", rc);
         std::lock_guard<std::mutex> lk(S->mu);
         if (rc != PXF_OK) {
             S->err = pxf_batch_last_error(S->batch);

@@ -120,3 +120,30 @@ def test_batch_autotune(lib):
     b.close()
     for s in sims:
         s.close()
+
+
+def test_batch_grows_and_shrinks_one_by_one(lib):
+    """Membership changing one simulation at a time (as the serving loop does) reallocates the
+    batch's tables repeatedly; every member still matches its own run."""
+    specs = [(dam(res=16 + 2 * k, ppc=4, iters=10), k, "pcg" if k % 2 else "gs") for k in range(7)]
+    n = len(specs)
+    ref = []
+    for k, sp in enumerate(specs):
+        with _make(sp) as s:
+            s.step(n - k)          # added k-th, then one batched substep after every addition
+            ref.append(s.read_particles())
+    sims = [_make(sp) for sp in specs]
+    b = P.Batch()
+    for s in sims:
+        b.add(s)
+        b.step(1)
+    b.sync()
+    for s, r in zip(sims, ref):
+        np.testing.assert_array_equal(s.read_particles(), r)
+    for s in sims[:5]:
+        b.remove(s)
+        b.step(1)
+    b.sync()
+    b.close()
+    for s in sims:
+        s.close()
