@@ -61,6 +61,7 @@ struct BatchImpl {
     uint32_t* d_base = nullptr;
     size_t cap_sims = 0;
     StageWork w_parts, w_tiles, w_cells, w_half, w_faces, w_chunks;
+    StageWork w_lchunks;                 // level-0 system-cell list chunks (PCG and the list GS)
     PcgWork pw;                          // precision-solver work indexes
     uint32_t max_gs_iters = 0;
     bool any_gs = false, any_pcg = false;
@@ -186,6 +187,7 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
     const uint64_t nc = uint64_t(n[0]) * n[1] * n[2];
     const uint64_t nf = uint64_t(n[0] + 1) * n[1] * n[2] + uint64_t(n[0]) * (n[1] + 1) * n[2] + uint64_t(n[0]) * n[1] * (n[2] + 1);
     const uint64_t nchunks = (nc + kScanChunk - 1) / kScanChunk;
+    const uint64_t lchunks = (nc + level0_chunk() - 1) / level0_chunk();
     Layout L{};
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t at = off; off += align256(bytes); return at; };
@@ -209,8 +211,8 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
     L.acc = o.keep_p2g_sums ? take(4 * nf) : 0;
     L.wacc = o.keep_p2g_sums ? take(4 * nf) : 0;
     // level-0 system-cell lists (red then black per chunk): both pressure solvers walk them
-    L.llist[0] = take(4 * nchunks * kScanChunk);
-    L.llcnt[0] = take(8 * nchunks);
+    L.llist[0] = take(4 * lchunks * level0_chunk());
+    L.llcnt[0] = take(8 * lchunks);
     const bool pcg = o.pressure_solver == PXF_PRESSURE_PCG;
     if (pcg) {
         L.x2 = take(8 * nc);
@@ -220,18 +222,18 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
         L.p0 = take(4 * nc);
         L.p1 = take(4 * nc);
         L.Ap = take(4 * nc);
-        L.partial = take(8 * nchunks);
+        L.partial = take(8 * lchunks);
         L.pcg = take(sizeof(PcgState));
         if (o.pcg_precond == 0) {
             L.nlev = mg_levels(n, L.dims);
             for (int l = 1; l < L.nlev; l++) {
                 const uint64_t c = uint64_t(L.dims[l][0]) * L.dims[l][1] * L.dims[l][2];
-                const uint64_t ch = (c + kCoarseChunk - 1) / kCoarseChunk;
+                const uint64_t ch = (c + coarse_chunk() - 1) / coarse_chunk();
                 L.ltype[l] = take(c);
                 L.linfo[l] = take(2 * c);
                 L.lr[l] = take(4 * c);
                 L.lz[l] = take(4 * c);
-                L.llist[l] = take(4 * ch * kCoarseChunk);
+                L.llist[l] = take(4 * ch * coarse_chunk());
                 L.llcnt[l] = take(8 * ch);
             }
         }
@@ -268,7 +270,7 @@ static inline uint32_t cdiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1
 
 // Work-index stages: particles, P2G tiles, cells, half cells, faces, 2048-cell chunks, then the
 // multigrid smoothing chunks of each level and the restriction chunks of each level.
-constexpr int kStages = 6 + 3 * kMaxLevels;
+constexpr int kStages = 7 + 3 * kMaxLevels;   // the last: level-0 list chunks
 
 int BatchImpl::rebuild() {
     cudaError_t e;
@@ -335,6 +337,7 @@ int BatchImpl::rebuild() {
             cdiv(uint64_t((d.nx + 1) / 2) * d.ny * d.nz, kElemItem),
             cdiv(d.nf, kElemItem),
             cdiv(d.nc, kScanChunk)};
+        items[kStages - 1] = cdiv(d.nc, d.lev[0].cs);
         const bool mg = d.solver == 1 && d.precond == 0;
         for (int l = 0; l < kMaxLevels; l++) {
             // global-memory smoothing of level l and restriction to l + 1 exist below the tail
@@ -371,6 +374,7 @@ int BatchImpl::rebuild() {
     if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "batch upload");
     StageWork* ws[kStages];
     ws[0] = &w_parts; ws[1] = &w_tiles; ws[2] = &w_cells; ws[3] = &w_half; ws[4] = &w_faces; ws[5] = &w_chunks;
+    ws[kStages - 1] = &w_lchunks;
     for (int l = 0; l < kMaxLevels; l++) {
         ws[6 + l] = &pw.level[l];
         ws[6 + kMaxLevels + l] = &pw.coarse[l];
@@ -390,8 +394,8 @@ int BatchImpl::rebuild() {
     }
     pw.sims = d_sims;
     pw.n_sims = n;
-    pw.chunks = w_chunks;
-    pw.chunks_all = w_chunks;
+    pw.chunks = w_lchunks;
+    pw.chunks_all = w_lchunks;
     // simulation of every item of every stage (one load instead of a search), for several simulations
     {
         size_t total = 0;
@@ -425,7 +429,7 @@ int BatchImpl::rebuild() {
             w->sim_of = n > 1 ? d_sim_of + off : nullptr;
             off += w->total;
         }
-        pw.chunks.sim_of = pw.chunks_all.sim_of = w_chunks.sim_of;
+        pw.chunks.sim_of = pw.chunks_all.sim_of = w_lchunks.sim_of;
         if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "item table upload");
     }
     // compacted item lists of the CG loop's stages (batches; PXF_CG_COMPACT=1 / 0 forces them on / off)
@@ -492,10 +496,10 @@ int BatchImpl::record_gs_part(cudaStream_t st) {
 cudaError_t BatchImpl::record_gs(cudaStream_t st) {
     static const bool dense = [] { const char* v = std::getenv("PXF_GS_DENSE"); return v && v[0] == '1'; }();
     cudaError_t e = cudaSuccess;
-    if (!dense && (e = launch_gs_lists(w_chunks, st)) != cudaSuccess) return e;
+    if (!dense && (e = launch_gs_lists(w_lchunks, st)) != cudaSuccess) return e;
     for (uint32_t it = 0; it < max_gs_iters; it++)
         for (uint32_t parity = 0; parity < 2; parity++) {
-            e = dense ? launch_pressure_rb(w_half, parity, it, st) : launch_pressure_rb_list(w_chunks, parity, it, st);
+            e = dense ? launch_pressure_rb(w_half, parity, it, st) : launch_pressure_rb_list(w_lchunks, parity, it, st);
             if (e != cudaSuccess) return e;
         }
     return e;
@@ -910,6 +914,22 @@ int BatchImpl::profile(pxf_stage_time* out, uint32_t cap, uint32_t* count) {
 
 void set_global_error_message(const std::string& m) { g_last_error = m; }
 
+static uint32_t chunk_env(const char* name, uint32_t dflt) {
+    const char* v = std::getenv(name);
+    const long k = v ? std::atol(v) : long(dflt);
+    return (k >= 256 && k <= 8192 && k % 256 == 0) ? uint32_t(k) : dflt;
+}
+
+uint32_t coarse_chunk() {
+    static const uint32_t cs = chunk_env("PXF_COARSE_CHUNK", 1024);
+    return cs;
+}
+
+uint32_t level0_chunk() {
+    static const uint32_t cs = chunk_env("PXF_L0_CHUNK", 4096);
+    return cs;
+}
+
 bool trace_on() {
     static const bool on = [] { const char* v = std::getenv("PXF_TRACE"); return v && v[0] == '1'; }();
     return on;
@@ -1070,7 +1090,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.lev[0].nc = d.nc;
     d.lev[0].type = d.type;
     d.lev[0].info = d.info;
-    d.lev[0].cs = kScanChunk;
+    d.lev[0].cs = level0_chunk();
     d.lev[0].list = reinterpret_cast<uint32_t*>(m + L.llist[0]);
     d.lev[0].lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[0]);
     if (opts.pressure_solver == PXF_PRESSURE_PCG) {
@@ -1096,7 +1116,7 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
             v.info = reinterpret_cast<uint16_t*>(m + L.linfo[l]);
             v.r = reinterpret_cast<float*>(m + L.lr[l]);
             v.z = reinterpret_cast<float*>(m + L.lz[l]);
-            v.cs = kCoarseChunk;
+            v.cs = coarse_chunk();
             v.list = reinterpret_cast<uint32_t*>(m + L.llist[l]);
             v.lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[l]);
         }

@@ -105,7 +105,7 @@ __device__ __forceinline__ float ldf(const float* p) { return __ldcg(p); }
 
 __device__ __forceinline__ bool active(const SimDev& s) { return s.solver == 1 && !ldu(&s.pcg->done); }
 
-__device__ __forceinline__ uint32_t nchunks0(const SimDev& s) { return (s.nc + kScanChunk - 1) / kScanChunk; }
+__device__ __forceinline__ uint32_t nchunks0(const SimDev& s) { return (s.nc + s.lev[0].cs - 1) / s.lev[0].cs; }
 
 // Fixed-order sum of a simulation's chunk partials (one block per simulation).
 __device__ __forceinline__ double sum_partials(const SimDev& s, double* sh) {
@@ -520,7 +520,7 @@ struct TailLevel {
     uint32_t nred, nsys;
 };
 
-constexpr uint32_t kTailMaxChunks = 64;   // list chunks per tail level (kTailCells / kCoarseChunk = 32)
+constexpr uint32_t kTailMaxChunks = 64;   // list chunks per tail level (kTailCells / 256 = 32 at most)
 
 __device__ void tail_smooth(const TailLevel& L, uint32_t color, int mode, const TailLevel* C) {
     const int nx = L.nx, ny = L.ny, nxy = L.nx * L.ny;
@@ -671,8 +671,9 @@ __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
             const uint32_t nch = nchunks0(*sp);
             for (uint32_t ch = 0; ch < nch; ch++) {
                 DF acc{0.f, 0.f};
-                const uint32_t end = min((ch + 1) * kScanChunk, sp->nc);
-                for (uint32_t c = ch * kScanChunk + threadIdx.x; c < end; c += blockDim.x)
+                const uint32_t cs0 = sp->lev[0].cs;
+                const uint32_t end = min((ch + 1) * cs0, sp->nc);
+                for (uint32_t c = ch * cs0 + threadIdx.x; c < end; c += blockDim.x)
                     if (lv[0].info[c]) acc = df_add(acc, two_prod(lv[0].r[c], lv[0].z[c]));
                 const double t = block_sum(acc, sh);
                 if (threadIdx.x == 0) sp->partial[ch] = t;
@@ -1002,8 +1003,9 @@ __device__ void ph_finish(const Work& w) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         if (s.solver != 1) continue;
-        for (uint32_t k = 0; k < kScanChunk / blockDim.x; k++) {
-            const uint32_t c = (item - w.base[si]) * kScanChunk + k * blockDim.x + threadIdx.x;
+        const uint32_t cs0 = s.lev[0].cs;
+        for (uint32_t k = 0; k < cs0 / blockDim.x; k++) {
+            const uint32_t c = (item - w.base[si]) * cs0 + k * blockDim.x + threadIdx.x;
             if (c >= s.nc) continue;
             double x = 0.0;
             if (in_system(s.info[c])) {
@@ -1618,7 +1620,7 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
         cudaError_t e;
         for (int l = 0; l + 1 < pw.max_levels; l++) {
             if (!pw.level[l].total) continue;
-            const uint32_t cs = l == 0 ? kScanChunk : kCoarseChunk;
+            const uint32_t cs = l == 0 ? level0_chunk() : coarse_chunk();
             size_t smem = 0;
             const unsigned g = coop_grid(pw.level[l], cs, &smem);
             if (g) {
@@ -1637,7 +1639,7 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
         launch_dep("k_mg_tail", k_mg_tail, pw.n_sims, 1024, pw.tail_smem, st, pw.sims, pw.n_sims);
         for (int l = pw.max_levels - 2; l >= 0; l--) {
             if (!pw.level[l].total) continue;
-            const uint32_t cs = l == 0 ? kScanChunk : kCoarseChunk;
+            const uint32_t cs = l == 0 ? level0_chunk() : coarse_chunk();
             size_t smem = 0;
             const unsigned g = coop_grid(pw.level[l], cs, &smem);
             if (g) {

@@ -74,7 +74,10 @@ constexpr uint32_t kTailCells = 8192;   // the shared-memory tail starts at the 
 static_assert(kTailCells <= 65536, "tail lists hold cell indices as 16-bit values");
 // Shared-memory floats a tail level of nc cells takes: r, z (float), neighbour record and list (u16).
 __host__ __device__ constexpr uint32_t tail_level_floats(uint32_t nc) { return 3 * nc; }
-constexpr uint32_t kCoarseChunk = 256;  // list chunk of the levels below level 0
+// List chunks (cells) of the system-cell lists: level 0 (PXF_L0_CHUNK) and the levels below it
+// (PXF_COARSE_CHUNK); multiples of 256 up to 8192, read once per process.
+uint32_t coarse_chunk();
+uint32_t level0_chunk();
 cudaError_t mg_tail_attr(size_t smem);
 
 // Grid barrier of the persistent solve (device memory, zeroed at every launch).
