@@ -76,6 +76,7 @@ struct BatchImpl {
     uint32_t* d_act = nullptr;           // compacted item lists of the CG loop's stages
     uint32_t* d_act_n = nullptr;
     size_t cap_act = 0;
+    uint32_t* d_tickets = nullptr;       // last-block tickets of the condition-setting control kernels
     cudaGraphExec_t exec = nullptr;
     bool dirty = true;
     bool cond_ok = true;                 // conditional while-node usable
@@ -109,7 +110,7 @@ struct BatchImpl {
     void drop_graphs();
     int profile(pxf_stage_time* out, uint32_t cap, uint32_t* count);
     int run_eager(KernelTimer* timer, pxf_tune_result* tune);
-    cudaError_t capture_restart(cudaStream_t st, int n);
+    cudaError_t capture_restart(cudaStream_t st, cudaGraphConditionalHandle h);
 };
 
 }  // namespace pxf
@@ -253,6 +254,7 @@ BatchImpl::~BatchImpl() {
     if (d_sim_of) cudaFree(d_sim_of);
     if (d_act) cudaFree(d_act);
     if (d_act_n) cudaFree(d_act_n);
+    if (d_tickets) cudaFree(d_tickets);
     if (side) cudaStreamDestroy(side);
     if (side2) cudaStreamDestroy(side2);
     if (stream) cudaStreamDestroy(stream);
@@ -471,6 +473,11 @@ int BatchImpl::rebuild() {
         if ((e = cudaMemset(d_bar, 0, 2 * sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
     }
     pw.sweep_bar = (pw.any_mg && d_bar) ? d_bar + 1 : nullptr;
+    if (any_pcg && !d_tickets) {
+        if ((e = cudaMalloc(&d_tickets, 2 * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "tickets");
+        if ((e = cudaMemset(d_tickets, 0, 2 * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "tickets");
+    }
+    pw.tickets = any_pcg ? d_tickets : nullptr;
     if (any_pcg) persist_grid = pcg_solve_grid(pw.tail_smem);
     trace("rebuild: indexes uploaded, capturing");
     int rc = capture();
@@ -534,17 +541,14 @@ int BatchImpl::record_post(cudaStream_t st) {
 
 // Inside the captured while body: `if (any simulation needs an FP64 restart) { restart kernels }`
 // as a nested IF node; plain (self-skipping) launches when nesting is unavailable.
-cudaError_t BatchImpl::capture_restart(cudaStream_t st, int n) {
-    if (!if_ok) return launch_pcg_restart(pw, st);
+// The restart kernels as an IF node whose condition the control kernel after the update set
+// (handle h, created on the body graph before that kernel).
+cudaError_t BatchImpl::capture_restart(cudaStream_t st, cudaGraphConditionalHandle h) {
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
-    cudaGraphConditionalHandle h;
     cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
-    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
-    if (e == cudaSuccess) e = launch_pcg_restart_cond(d_sims, n, h, st);
-    if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
     alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
     std::memset(np_raw, 0, sizeof(np_raw));
     cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_raw);
@@ -644,14 +648,23 @@ int BatchImpl::capture() {
                 cudaGraph_t body = np.conditional.phGraph_out[0];
                 e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
                 if (e == cudaSuccess) {
+                    // body: direction, update (its control kernel sets the restart IF), the restart
+                    // IF node, the preconditioner (its control kernel sets the loop condition)
                     cudaError_t e1 = launch_pcg_dir(pw, side);
-                    if (e1 == cudaSuccess) e1 = launch_pcg_update(pw, side);
-                    if (e1 == cudaSuccess) e1 = capture_restart(side, n);
-                    if (e1 == cudaSuccess) e1 = launch_precond(pw, side);
-                    cudaError_t e2 = launch_pcg_cond(d_sims, n, h, side);
+                    cudaGraphConditionalHandle hif = 0;
+                    if (e1 == cudaSuccess && if_ok) {
+                        cudaStreamCaptureStatus bs;
+                        cudaGraph_t bg = nullptr;
+                        e1 = cudaStreamGetCaptureInfo(side, &bs, nullptr, &bg, nullptr, nullptr, nullptr);
+                        if (e1 == cudaSuccess) e1 = cudaGraphConditionalHandleCreate(&hif, bg, 0, cudaGraphCondAssignDefault);
+                        if (e1 != cudaSuccess) if_ok = false;
+                    }
+                    if (e1 == cudaSuccess) e1 = if_ok ? launch_pcg_update(pw, side, hif, d_tickets) : launch_pcg_update(pw, side);
+                    if (e1 == cudaSuccess) e1 = if_ok ? capture_restart(side, hif) : launch_pcg_restart(pw, side);
+                    if (e1 == cudaSuccess) e1 = launch_precond(pw, side, h, d_tickets + 1);
                     cudaGraph_t out = body;
                     cudaError_t e3 = cudaStreamEndCapture(side, &out);
-                    e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+                    e = e1 != cudaSuccess ? e1 : e3;
                 }
             }
             if (e != cudaSuccess) cond_failed = true;

@@ -1178,7 +1178,26 @@ __global__ void __launch_bounds__(THREADS) k_pcg_resid(Work w) { ph_resid(w); de
 __global__ void __launch_bounds__(THREADS) k_pcg_dir(Work w) { ph_dir(w); dep_wait(); }
 __global__ void __launch_bounds__(THREADS) k_pcg_update(Work w) { ph_update(w); dep_wait(); }
 __global__ void __launch_bounds__(THREADS) k_pcg_finish(Work w) { ph_finish(w); }
-__global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_sims, int phase) { ph_ctl(sims, n_sims, phase); }
+// With a ticket, the block that finishes last also sets the loop's conditional handle: after a
+// restart decision (phase 4) whether any simulation restarts, after r.z (phase 2) whether any is
+// still solving. Each block publishes its state (fence) before taking its ticket, and the last one
+// resets the ticket for the next use.
+__global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_sims, int phase,
+                                                     cudaGraphConditionalHandle h, uint32_t* ticket) {
+    ph_ctl(sims, n_sims, phase);
+    if (!ticket) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        if (t == gridDim.x - 1) {
+            __threadfence();
+            const bool any = phase == 4 ? any_restart(sims, n_sims) : any_active(sims, n_sims);
+            cudaGraphSetConditional(h, any ? 1u : 0u);
+            *ticket = 0;
+        }
+    }
+}
 
 __global__ void k_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -1537,8 +1556,9 @@ static void launch_dep(const char* name, void (*k)(KArgs...), unsigned grid, uns
     note_launch(name, st);
 }
 
-static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st) {
-    launch_dep("k_pcg_ctl", k_pcg_ctl, pw.n_sims, THREADS, 0, st, pw.sims, pw.n_sims, phase);
+static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st, cudaGraphConditionalHandle h = 0,
+                       uint32_t* ticket = nullptr) {
+    launch_dep("k_pcg_ctl", k_pcg_ctl, pw.n_sims, THREADS, 0, st, pw.sims, pw.n_sims, phase, h, ticket);
     return cudaGetLastError();
 }
 
@@ -1611,7 +1631,7 @@ static bool coop_smoothing() {
     return v && v[0] == '1';
 }
 
-cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
+cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st, cudaGraphConditionalHandle h, uint32_t* ticket) {
     if (pw.any_jacobi) {
         launch_dep("k_jacobi", k_jacobi, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
     }
@@ -1677,7 +1697,7 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st) {
             }
         }
     }
-    return ctl(pw, 2, st);
+    return ctl(pw, 2, st, h, ticket);
 }
 
 cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st) {
@@ -1687,6 +1707,10 @@ cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st) {
 }
 
 cudaError_t launch_pcg_init(const PcgWork& pw, cudaStream_t st) {
+    if (pw.tickets) {
+        cudaError_t e = cudaMemsetAsync(pw.tickets, 0, 2 * sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+    }
     launch_mg_setup(pw, st);
     k_pcg_init<<<grid_w(pw.chunks), THREADS, 0, st>>>(mkw(pw.chunks)); note_launch("k_pcg_init", st);
     ctl(pw, 0, st);
@@ -1699,9 +1723,9 @@ cudaError_t launch_pcg_dir(const PcgWork& pw, cudaStream_t st) {
     return ctl(pw, 3, st);
 }
 
-cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st) {
+cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st, cudaGraphConditionalHandle h, uint32_t* ticket) {
     launch_dep("k_pcg_update", k_pcg_update, grid_w(pw.chunks), THREADS, 0, st, mkw(pw.chunks));
-    return ctl(pw, 4, st);
+    return ctl(pw, 4, st, h, ticket);
 }
 
 cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st) {

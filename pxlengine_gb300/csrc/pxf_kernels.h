@@ -63,6 +63,7 @@ struct PcgWork {
     StageWork setup[kMaxLevelsK];     // level-(l+1) chunks of every multigrid simulation with level l+1
     uint32_t* act_n = nullptr;        // counters: [0] chunks, [1 + l] level[l], [1 + kMaxLevelsK + l] coarse[l]
     struct GridBar* sweep_bar = nullptr;  // grid barrier of the cooperative smoothing kernels
+    uint32_t* tickets = nullptr;          // [2] last-block tickets of the control kernels that set conditions
     int setup_levels = 0;
     int max_levels = 0;                 // global-memory levels (below the shared-memory tail)
     int max_pairs = 1;                  // largest smoothing pair count of the batch's multigrid simulations
@@ -105,9 +106,13 @@ cudaError_t launch_pcg_solve(const PcgWork& pw, GridBar* bar, int grid, uint32_t
 cudaError_t launch_pcg_init(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_dir(const PcgWork& pw, cudaStream_t st);
-cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st);
+// With a handle and a ticket the control kernel after the update also sets the restart IF node's
+// condition (launch_pcg_update) or the loop's WHILE condition (launch_precond).
+cudaError_t launch_pcg_update(const PcgWork& pw, cudaStream_t st, cudaGraphConditionalHandle h = 0,
+                              uint32_t* ticket = nullptr);
 cudaError_t launch_pcg_restart(const PcgWork& pw, cudaStream_t st);
-cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st);
+cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st, cudaGraphConditionalHandle h = 0,
+                           uint32_t* ticket = nullptr);
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
 // Sets an IF condition: does any simulation need an FP64 restart residual now?
