@@ -160,19 +160,44 @@ __global__ void __launch_bounds__(256) k_scan_apply(Work w) {
 // ------------------------------------------------------------------ counting sort: scatter
 // B[start[cell] + rank] = A. The cell is recomputed from the position with the same expression
 // that produced the rank, so it matches bit for bit.
+// Four items per block pass (grid-strided), every load of the four issued before any store, so
+// each thread keeps four particles in flight.
 __global__ void __launch_bounds__(256) k_scatter(Work w) {
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
-        const int si = find_sim(w, item);
-        const SimDev s = w.sims[si];
-        const uint32_t i = (item - w.base[si]) * 256 + threadIdx.x;
-        if (i >= s.np) continue;
-        const float4 P = s.posA[i];
-        const float4 V = s.velA[i];
-        const uint32_t c = cell_of(s, P.x, P.y, P.z);
-        const uint32_t dst = s.start[c] + __float_as_uint(V.w);
-        if (dst < s.np) {   // always true when the ranks come from the last binning
-            s.posB[dst] = P;
-            s.velB[dst] = V;
+    constexpr int U = 4;
+    for (uint32_t item0 = blockIdx.x; item0 < w.total; item0 += U * gridDim.x) {
+        float4 P[U], V[U];
+        const SimDev* sp[U];
+        uint32_t idx[U];
+        bool live[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint32_t item = item0 + u * gridDim.x;
+            live[u] = false;
+            sp[u] = w.sims;
+            idx[u] = 0;
+            if (item >= w.total) continue;
+            const int si = find_sim(w, item);
+            sp[u] = w.sims + si;
+            idx[u] = (item - w.base[si]) * 256 + threadIdx.x;
+            live[u] = idx[u] < sp[u]->np;
+            if (live[u]) {
+                P[u] = sp[u]->posA[idx[u]];
+                V[u] = sp[u]->velA[idx[u]];
+            }
+        }
+        uint32_t dst[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            dst[u] = 0xffffffffu;
+            if (!live[u]) continue;
+            const SimDev& s = *sp[u];
+            dst[u] = s.start[cell_of(s, P[u].x, P[u].y, P[u].z)] + __float_as_uint(V[u].w);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (!live[u] || dst[u] >= sp[u]->np) continue;   // always below np when the ranks come from the last binning
+            sp[u]->posB[dst[u]] = P[u];
+            sp[u]->velB[dst[u]] = V[u];
         }
     }
 }
