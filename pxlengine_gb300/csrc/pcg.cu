@@ -1204,11 +1204,6 @@ __global__ void k_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalH
     cudaGraphSetConditional(h, any_active(sims, n_sims) ? 1u : 0u);
 }
 
-__global__ void k_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    cudaGraphSetConditional(h, any_restart(sims, n_sims) ? 1u : 0u);
-}
-
 __global__ void k_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     *flag = any_active(sims, n_sims) ? 1u : 0u;
@@ -1733,11 +1728,6 @@ cudaError_t launch_pcg_body(const PcgWork& pw, cudaStream_t st) {
     launch_pcg_update(pw, st);
     launch_pcg_restart(pw, st);
     return launch_precond(pw, st);
-}
-
-cudaError_t launch_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {
-    k_pcg_restart_cond<<<1, 32, 0, st>>>(sims, n_sims, h); note_launch("k_pcg_restart_cond", st);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st) {

@@ -47,7 +47,7 @@ struct MgLevel {
     uint16_t* info;
     float* r;
     float* z;
-    // System cells of each chunk of `cs` cells (2048 on level 0, 256 below), in ascending order:
+    // System cells of each chunk of `cs` cells (level0_chunk() on level 0, coarse_chunk() below), in ascending order:
     // chunk k owns list[cs k ...], first its red cells ((i + j + k) even), then its black cells;
     // lcnt[2k], lcnt[2k+1] count them.
     uint32_t cs;
@@ -80,7 +80,7 @@ struct SimDev {
     float2* x2;              // solution as a double-float pair (hi, lo)
     double* x64;             // FP64 solution, written at restarts and at the end of the solve
     float *r, *z, *p0, *p1, *Ap;
-    double* partial;         // two partial sums per 2048-cell chunk of level 0
+    double* partial;         // one partial sum per list chunk of level 0
     PcgState* pcg;
     int nlev;
     int tail;                // first level handled by the shared-memory tail kernel

@@ -10,7 +10,7 @@ namespace pxf {
 // Device-resident work index of one stage.
 using StageWork = Work;
 
-constexpr uint32_t kScanChunk = 2048;     // cells per scan / precision-solver work item
+constexpr uint32_t kScanChunk = 2048;     // cells per work item of the counting-sort scan
 constexpr uint32_t kElemItem = 256;       // elements per item of the per-element kernels
 constexpr int kMaxLevelsK = 12;           // multigrid levels (kMaxLevels in pxf_device.cuh)
 
@@ -116,7 +116,6 @@ cudaError_t launch_precond(const PcgWork& pw, cudaStream_t st, cudaGraphConditio
 cudaError_t launch_pcg_finish(const PcgWork& pw, cudaStream_t st);
 cudaError_t launch_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
 // Sets an IF condition: does any simulation need an FP64 restart residual now?
-cudaError_t launch_pcg_restart_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h, cudaStream_t st);
 // Host-driven fallback: a flag telling whether any simulation still runs.
 cudaError_t launch_pcg_any(const SimDev* sims, int n_sims, uint32_t* flag, cudaStream_t st);
 
