@@ -460,45 +460,53 @@ __device__ void ph_restrict(const Work& w, int l) {
         uint32_t lo, hi;
         seg(Cc, chunk, 2, lo, hi);
         const uint32_t* lst = list_of(Cc, chunk);
-        dep_wait();
-        if (ldu(&sp->pcg->done)) continue;
-        const uint32_t chd = threadIdx.x & 7u;
-        const uint32_t per_pass = blockDim.x / 8;
         // Below the tail, level l+1's first half sweep (red from zero: z = r / cnt) is done here.
         const bool first_sweep = l + 1 < sp->tail;
-        for (uint32_t base = lo; base < hi; base += per_pass) {
-            const uint32_t e = base + (threadIdx.x >> 3);
-            float res = 0.0f;
-            uint32_t P = 0;
+        // One coarse cell per thread. Its first pass reads the children's records (fixed during
+        // the solve) before dep_wait().
+        bool waited = false;
+        for (uint32_t e = lo + threadIdx.x; e < hi || (!waited && e == lo + threadIdx.x); e += blockDim.x) {
+            const bool h = e < hi;
+            uint32_t P = 0, cc[8], inf[8];
             bool red = false;
-            if (e < hi) {
-                P = lst[e];
+            if (h) {
+                P = __ldcg(lst + e);
                 const int I = int(P % uint32_t(Cc.nx)), J = int((P / uint32_t(Cc.nx)) % uint32_t(Cc.ny));
                 const int K = int(P / (uint32_t(Cc.nx) * uint32_t(Cc.ny)));
                 red = ((I + J + K) & 1) == 0;
-                const int i = 2 * I + int(chd & 1u), j = 2 * J + int((chd >> 1) & 1u), kk = 2 * K + int(chd >> 2);
-                if (i < F.nx && j < F.ny && kk < F.nz) {
-                    const uint32_t c = uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk);
-                    const uint32_t inf = F.info[c];
-                    if (in_system(inf)) {
-                        float az = cnt_of(inf) * F.z[c];
 #pragma unroll
-                        for (int q = 0; q < 6; q++)
-                            if (inf & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
-                        res = F.r[c] - az;
-                    }
+                for (int chd = 0; chd < 8; chd++) {
+                    const int i = 2 * I + (chd & 1), j = 2 * J + ((chd >> 1) & 1), kk = 2 * K + (chd >> 2);
+                    const bool in = i < F.nx && j < F.ny && kk < F.nz;
+                    cc[chd] = in ? uint32_t(i) + nx * uint32_t(j) + nxy * uint32_t(kk) : 0u;
+                    inf[chd] = in ? uint32_t(F.info[cc[chd]]) : 0u;
                 }
             }
-            // ((c0 + c1) + (c2 + c3)) + ((c4 + c5) + (c6 + c7))
-            res += __shfl_down_sync(0xffffffffu, res, 1, 8);
-            res += __shfl_down_sync(0xffffffffu, res, 2, 8);
-            res += __shfl_down_sync(0xffffffffu, res, 4, 8);
-            if (e < hi && chd == 0) {
-                const float rc = 0.5f * res;
-                Cc.r[P] = rc;
-                if (first_sweep && red) Cc.z[P] = rc / cnt_of(Cc.info[P]);
+            if (!waited) {
+                dep_wait();
+                waited = true;
+                if (ldu(&sp->pcg->done)) break;
             }
+            if (!h) continue;
+            float res[8];
+#pragma unroll
+            for (int chd = 0; chd < 8; chd++) {
+                res[chd] = 0.0f;
+                if (!in_system(inf[chd])) continue;
+                const uint32_t c = cc[chd];
+                float az = cnt_of(inf[chd]) * F.z[c];
+#pragma unroll
+                for (int q = 0; q < 6; q++)
+                    if (inf[chd] & (1u << q)) az -= F.z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
+                res[chd] = F.r[c] - az;
+            }
+            // ((c0 + c1) + (c2 + c3)) + ((c4 + c5) + (c6 + c7))
+            const float sum = ((res[0] + res[1]) + (res[2] + res[3])) + ((res[4] + res[5]) + (res[6] + res[7]));
+            const float rc = 0.5f * sum;
+            Cc.r[P] = rc;
+            if (first_sweep && red) Cc.z[P] = rc / cnt_of(Cc.info[P]);
         }
+        if (!waited) dep_wait();
     }
 }
 
