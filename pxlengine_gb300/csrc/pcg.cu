@@ -314,37 +314,9 @@ __device__ void ph_info(const Work& w, int l) {
 // mode 0: z = (r + sum z_n) / cnt; mode 1: the other colour is zero (z = r / cnt);
 // mode 2: as 0 with the coarse correction of level l+1 added to every neighbour on the fly
 // (fused prolongation); mode 3: as 0, then the chunk's partial r.z over all system cells.
-// One cell's update: (r + sum of its system neighbours' z, plus in mode 2 each neighbour's coarse
-// correction) / cnt.
-__device__ __forceinline__ float smooth_cell(uint32_t c, uint32_t inf, float rc, const float* __restrict__ z,
-                                             int mode, uint32_t nx, uint32_t ny, uint32_t nxy, const MgLevel& Cc,
-                                             uint32_t cnx, uint32_t cnxy) {
-    float sum = rc;
-    if (mode == 2) {
-        const uint32_t i = c % nx, j = (c / nx) % ny, kk = c / nxy;
-#pragma unroll
-        for (int q = 0; q < 6; q++) {
-            if (!(inf & (1u << q))) continue;
-            const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
-            const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
-            const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
-            const uint32_t n = uint32_t(int64_t(c) + dx + int64_t(dy) * nx + int64_t(dz) * nxy);
-            float zn = z[n];
-            const uint32_t P = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
-                               cnxy * (uint32_t(int(kk) + dz) >> 1);
-            if (in_system(Cc.info[P])) zn += Cc.z[P];
-            sum += zn;
-        }
-    } else if (mode != 1) {
-#pragma unroll
-        for (int q = 0; q < 6; q++)
-            if (inf & (1u << q)) sum += z[uint32_t(int64_t(c) + nbr(q, nx, nxy))];
-    }
-    return sum / cnt_of(inf);
-}
-
 __device__ void ph_smooth(const Work& w, int l, int color, int mode_in, int pass) {
     __shared__ double sh[32];
+    constexpr int SE = 1;   // entries per thread whose operands are in flight together
     for (uint32_t w_k = blockIdx.x, w_n = work_count(w); w_k < w_n; w_k += gridDim.x) {
         const uint32_t item = work_item(w, w_k);
         const int si = find_sim(w, item);
@@ -361,75 +333,86 @@ __device__ void ph_smooth(const Work& w, int l, int color, int mode_in, int pass
         seg(L, chunk, color, lo, hi);
         const uint32_t* __restrict__ lst = list_of(L, chunk);
         const uint16_t* __restrict__ info = L.info;
-        // this thread's first entry and its record are fixed during the solve: read before the wait
-        const uint32_t e0 = lo + threadIdx.x;
-        const bool h0 = e0 < hi;
-        const uint32_t c0 = h0 ? __ldcg(lst + e0) : 0u;
-        const uint32_t i0 = h0 ? uint32_t(info[c0]) : 0u;
-        // mode 2: the coarse cells above the first cell's neighbours and whether they are in the
-        // coarse system (both fixed during the solve)
-        uint32_t P[6] = {0, 0, 0, 0, 0, 0};
-        uint32_t pin = 0;
-        if (h0 && mode == 2) {
-            const uint32_t i = c0 % nx, j = (c0 / nx) % ny, kk = c0 / nxy;
-#pragma unroll
-            for (int q = 0; q < 6; q++) {
-                if (!(i0 & (1u << q))) continue;
-                const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
-                const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
-                const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
-                P[q] = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
-                       cnxy * (uint32_t(int(kk) + dz) >> 1);
-                if (in_system(Cc.info[P[q]])) pin |= 1u << q;
-            }
-        }
-        dep_wait();
         const float* __restrict__ r = L.r;
         float* __restrict__ z = L.z;
-        // every value the first cell needs, issued together with the convergence flag
-        const uint32_t done = ldu(&sp->pcg->done);
-        float r0 = 0.0f, zn[6], zc[6];
+        bool waited = false;
+        bool stop = false;
+        for (uint32_t e0 = lo + threadIdx.x; !stop && (e0 < hi || !waited); e0 += SE * blockDim.x) {
+            // fixed during the solve: list entries, records and, for mode 2, the coarse cells above
+            // the neighbours and whether they are in the coarse system
+            uint32_t cc[SE], ii[SE], pin[SE], P[SE][6];
+            bool hh[SE];
 #pragma unroll
-        for (int q = 0; q < 6; q++) {
-            zn[q] = 0.0f;
-            zc[q] = 0.0f;
-        }
-        if (h0) {
-            r0 = r[c0];
-            if (mode != 1) {
+            for (int u = 0; u < SE; u++) {
+                const uint32_t e = e0 + u * blockDim.x;
+                hh[u] = e < hi;
+                cc[u] = hh[u] ? __ldcg(lst + e) : 0u;
+                ii[u] = hh[u] ? uint32_t(info[cc[u]]) : 0u;
+                pin[u] = 0;
 #pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (i0 & (1u << q)) zn[q] = z[uint32_t(int64_t(c0) + nbr(q, nx, nxy))];
-            }
-            if (mode == 2) {
+                for (int q = 0; q < 6; q++) P[u][q] = 0;
+                if (hh[u] && mode == 2) {
+                    const uint32_t c = cc[u], i = c % nx, j = (c / nx) % ny, kk = c / nxy;
 #pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (pin & (1u << q)) zc[q] = Cc.z[P[q]];
-            }
-        }
-        if (done) continue;
-        if (h0) {
-            // the same sums, in the same order, as smooth_cell
-            float sum = r0;
-            if (mode == 2) {
-#pragma unroll
-                for (int q = 0; q < 6; q++) {
-                    if (!(i0 & (1u << q))) continue;
-                    float t = zn[q];
-                    if (pin & (1u << q)) t += zc[q];
-                    sum += t;
+                    for (int q = 0; q < 6; q++) {
+                        if (!(ii[u] & (1u << q))) continue;
+                        const int dx = q == 0 ? -1 : (q == 1 ? 1 : 0);
+                        const int dy = q == 2 ? -1 : (q == 3 ? 1 : 0);
+                        const int dz = q == 4 ? -1 : (q == 5 ? 1 : 0);
+                        P[u][q] = (uint32_t(int(i) + dx) >> 1) + cnx * (uint32_t(int(j) + dy) >> 1) +
+                                  cnxy * (uint32_t(int(kk) + dz) >> 1);
+                        if (in_system(Cc.info[P[u][q]])) pin[u] |= 1u << q;
+                    }
                 }
-            } else if (mode != 1) {
-#pragma unroll
-                for (int q = 0; q < 6; q++)
-                    if (i0 & (1u << q)) sum += zn[q];
             }
-            z[c0] = sum / cnt_of(i0);
+            if (!waited) {
+                dep_wait();
+                waited = true;
+                if (ldu(&sp->pcg->done)) { stop = true; break; }
+            }
+            // every operand of the entries, issued before any store
+            float rv[SE], zn[SE][6], zc[SE][6];
+#pragma unroll
+            for (int u = 0; u < SE; u++) {
+                rv[u] = 0.0f;
+#pragma unroll
+                for (int q = 0; q < 6; q++) { zn[u][q] = 0.0f; zc[u][q] = 0.0f; }
+                if (!hh[u]) continue;
+                rv[u] = r[cc[u]];
+                if (mode != 1) {
+#pragma unroll
+                    for (int q = 0; q < 6; q++)
+                        if (ii[u] & (1u << q)) zn[u][q] = z[uint32_t(int64_t(cc[u]) + nbr(q, nx, nxy))];
+                }
+                if (mode == 2) {
+#pragma unroll
+                    for (int q = 0; q < 6; q++)
+                        if (pin[u] & (1u << q)) zc[u][q] = Cc.z[P[u][q]];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < SE; u++) {
+                if (!hh[u]) continue;
+                // the reference's sums: r, then each system neighbour's z (plus its parent's
+                // correction in mode 2), in neighbour order
+                float sum = rv[u];
+                if (mode == 2) {
+#pragma unroll
+                    for (int q = 0; q < 6; q++) {
+                        if (!(ii[u] & (1u << q))) continue;
+                        float t = zn[u][q];
+                        if (pin[u] & (1u << q)) t += zc[u][q];
+                        sum += t;
+                    }
+                } else if (mode != 1) {
+#pragma unroll
+                    for (int q = 0; q < 6; q++)
+                        if (ii[u] & (1u << q)) sum += zn[u][q];
+                }
+                z[cc[u]] = sum / cnt_of(ii[u]);
+            }
         }
-        for (uint32_t e = e0 + blockDim.x; e < hi; e += blockDim.x) {
-            const uint32_t c = lst[e];
-            z[c] = smooth_cell(c, info[c], r[c], z, mode, nx, ny, nxy, Cc, cnx, cnxy);
-        }
+        if (stop) continue;
         if (mode == 3) {
             // r.z over every system cell of the chunk (the other colour was final before this sweep).
             __syncthreads();
