@@ -1404,7 +1404,7 @@ __device__ __forceinline__ void coop_sweep(const Work& lw, int l, int color, int
 #pragma unroll
         for (int j = 0; j < J; j++) {
             if (!ii[j]) continue;
-            // smooth_cell's sums, in its order
+            // the same sums, in the same order, as ph_smooth
             float sum = rv[j];
             if (mode[j] == 2) {
 #pragma unroll
