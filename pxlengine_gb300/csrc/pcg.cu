@@ -511,7 +511,8 @@ struct TailLevel {
     uint32_t nred, nsys;
 };
 
-constexpr uint32_t kTailMaxChunks = 64;   // list chunks per tail level (kTailCells / 256 = 32 at most)
+constexpr uint32_t kTailMaxChunks = 32;   // list chunks per tail level (kTailCells / 256 at most)
+constexpr int kTailMaxLevels = 6;         // tail levels: kTailCells down to the coarsest (<= 512 cells)
 
 __device__ void tail_smooth(const TailLevel& L, uint32_t color, int mode, const TailLevel* C) {
     const int nx = L.nx, ny = L.ny, nxy = L.nx * L.ny;
@@ -574,16 +575,19 @@ __device__ void tail_restrict(const TailLevel& F, const TailLevel& Cc) {
 
 __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
     __shared__ double sh[32];
-    __shared__ uint32_t cr[kTailMaxChunks], cb[kTailMaxChunks], orr[kTailMaxChunks], obb[kTailMaxChunks];
-    __shared__ uint32_t tot[2];
+    // per tail level: list counts of its chunks and their offsets in the gathered list
+    __shared__ uint32_t cr[kTailMaxLevels][kTailMaxChunks], cb[kTailMaxLevels][kTailMaxChunks];
+    __shared__ uint32_t orr[kTailMaxLevels][kTailMaxChunks], obb[kTailMaxLevels][kTailMaxChunks];
+    __shared__ uint32_t tot[kTailMaxLevels][2];
     for (int si = blockIdx.x; si < n_sims; si += gridDim.x) {
         const SimDev* sp = sims + si;
         if (sp->solver != 1 || sp->precond != 0) continue;
         const int T = sp->tail, NL = sp->nlev;
         TailLevel lv[kMaxLevels];
         float* base = tsm;
+        // all levels at once, in three steps: records and list counts, offsets, list entries
         for (int l = T; l < NL; l++) {
-            const MgLevel g = sp->lev[l];
+            const MgLevel& g = sp->lev[l];
             TailLevel& t = lv[l];
             t.nx = g.nx; t.ny = g.ny; t.nz = g.nz; t.nc = g.nc;
             t.r = base;
@@ -595,30 +599,38 @@ __device__ void ph_tail(const SimDev* sims, int n_sims, float* tsm) {
                 const uint32_t inf = __ldcg(g.info + c);
                 t.info[c] = in_system(inf) ? uint16_t(inf) : uint16_t(0);
             }
-            // gather the per-chunk red / black lists into one list
             const uint32_t nch = (g.nc + g.cs - 1) / g.cs;
             for (uint32_t k = threadIdx.x; k < nch; k += blockDim.x) {
-                cr[k] = __ldcg(g.lcnt + 2 * k);
-                cb[k] = __ldcg(g.lcnt + 2 * k + 1);
+                cr[l - T][k] = __ldcg(g.lcnt + 2 * k);
+                cb[l - T][k] = __ldcg(g.lcnt + 2 * k + 1);
             }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                uint32_t a = 0, b = 0;
-                for (uint32_t k = 0; k < nch; k++) { orr[k] = a; a += cr[k]; }
-                for (uint32_t k = 0; k < nch; k++) { obb[k] = a + b; b += cb[k]; }
-                tot[0] = a;
-                tot[1] = a + b;
-            }
-            __syncthreads();
-            t.nred = tot[0];
-            t.nsys = tot[1];
+        }
+        __syncthreads();
+        if (int(threadIdx.x) < NL - T) {
+            const int lt = int(threadIdx.x);
+            const MgLevel& g = sp->lev[T + lt];
+            const uint32_t nch = (g.nc + g.cs - 1) / g.cs;
+            uint32_t a = 0, b = 0;
+            for (uint32_t k = 0; k < nch; k++) { orr[lt][k] = a; a += cr[lt][k]; }
+            for (uint32_t k = 0; k < nch; k++) { obb[lt][k] = a + b; b += cb[lt][k]; }
+            tot[lt][0] = a;
+            tot[lt][1] = a + b;
+        }
+        __syncthreads();
+        for (int l = T; l < NL; l++) {
+            const MgLevel& g = sp->lev[l];
+            TailLevel& t = lv[l];
+            const int lt = l - T;
+            t.nred = tot[lt][0];
+            t.nsys = tot[lt][1];
+            const uint32_t nch = (g.nc + g.cs - 1) / g.cs;
             for (uint32_t e = threadIdx.x; e < nch * g.cs; e += blockDim.x) {
                 const uint32_t k = e / g.cs, m = e - k * g.cs;
-                if (m < cr[k]) t.list[orr[k] + m] = uint16_t(__ldcg(g.list + e));
-                else if (m < cr[k] + cb[k]) t.list[obb[k] + m - cr[k]] = uint16_t(__ldcg(g.list + e));
+                if (m < cr[lt][k]) t.list[orr[lt][k] + m] = uint16_t(__ldcg(g.list + e));
+                else if (m < cr[lt][k] + cb[lt][k]) t.list[obb[lt][k] + m - cr[lt][k]] = uint16_t(__ldcg(g.list + e));
             }
-            __syncthreads();
         }
+        __syncthreads();
         // everything above is fixed during the solve; r is the previous kernel's output
         dep_wait();
         if (__ldcg(&sp->pcg->done)) {
