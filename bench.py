@@ -163,7 +163,10 @@ def kernel_bytes(kernel, N, F, C, Cf, lv=None):
         # fine r, z, record in (10 B per fine system cell); coarse list in, r and red z out
         return sum(10 * cf[l] + 10 * cf[l + 1] for l in range(T)) / T
     return {
+        "k_scan_chunks": 4 * C,                      # counts in (chunk sums out)
         "k_scan_apply": 4 * C + 4 * C + 1 * C,       # counts in; starts and cell flags out
+        "k_gs_lists": 2 * C + 4 * Cf,                # neighbour records in; system-cell lists out
+        "k_cell_lists": 2 * C + 4 * Cf,
         "k_scatter": 64 * N,                         # particle records in and out (sorted order)
         "k_p2g": 32 * N + 8 * F + 4 * C,             # sorted particles and cell starts in; vel, vel_old out
         "k_divergence": 4 * F + 1 * C + 4 * C + 2 * C,   # faces, flags in; divergence, neighbour record out
@@ -511,7 +514,14 @@ def main():
     if not args.no_profile:
         prof = sim.profile_substep()
         total = sum(r[2] for r in prof)
-        kernels = [{"kernel": n, "launches": k, "ms": m, "share": m / total} for n, k, m in prof]
+        kernels = []
+        for n, k, m in prof:
+            rec = {"kernel": n, "launches": k, "ms": m, "share": m / total}
+            b = kernel_bytes(n, N, F, C, Cf, lv)
+            if b:
+                gbs = b / (m / k / 1e3) / 1e9
+                rec.update({"alg_bytes_per_launch": b, "achieved_gbs": gbs, "frac_of_peak": gbs / peak})
+            kernels.append(rec)
         ranked = sorted(prof, key=lambda r: -r[2])
         top = next((r for r in ranked if kernel_bytes(r[0], N, F, C, Cf, lv)), None)
         if top:

@@ -103,19 +103,31 @@ __global__ void __launch_bounds__(1024) k_scan_sims(const SimDev* sims, int n_si
 
 // start = exclusive scan of count; count := 0 for the next binning; cell type and the pressure
 // reset of normalize_grid (fluid.slang:125-131).
+// Counts are read and starts, flags and resets written in coalesced passes (cell k*256 + tid of the
+// chunk); the exclusive scan runs over each thread's 8 consecutive cells staged in shared memory
+// (one padding word per 32 keeps those reads free of bank conflicts).
 __global__ void __launch_bounds__(256) k_scan_apply(Work w) {
     __shared__ uint32_t wsum[8];
+    __shared__ uint32_t sv[SCAN_CHUNK + SCAN_CHUNK / 32];   // counts, then exclusive starts
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         const uint32_t chunk = item - w.base[si];
-        const uint32_t c0 = chunk * SCAN_CHUNK + threadIdx.x * 8;
+        const uint32_t cbase = chunk * SCAN_CHUNK;
+        auto slot = [](uint32_t o) { return o + (o >> 5); };
+        uint32_t vk[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t o = uint32_t(k) * 256 + threadIdx.x;
+            vk[k] = cbase + o < s.nc ? s.count[cbase + o] : 0u;
+            sv[slot(o)] = vk[k];
+        }
+        __syncthreads();
         uint32_t v[8];
         uint32_t tsum = 0;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            uint32_t c = c0 + k;
-            v[k] = c < s.nc ? s.count[c] : 0u;
+            v[k] = sv[slot(threadIdx.x * 8 + k)];
             tsum += v[k];
         }
         const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -130,26 +142,31 @@ __global__ void __launch_bounds__(256) k_scan_apply(Work w) {
         uint32_t before = s.chunk[chunk];
         for (int k = 0; k < wid; k++) before += wsum[k];
         before += x - tsum;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            sv[slot(threadIdx.x * 8 + k)] = before;
+            before += v[k];
+        }
+        __syncthreads();
         const uint32_t nxy = uint32_t(s.nx) * uint32_t(s.ny);
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const uint32_t c = c0 + k;
-            if (c < s.nc) {
-                s.start[c] = before;
-                before += v[k];
-                s.count[c] = 0;
-                if (v[k] > kPackedMaxPerCell) atomicOr(&s.chunk[(s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK], 1u);
-                const int i = int(c % uint32_t(s.nx));
-                const int j = int((c / uint32_t(s.nx)) % uint32_t(s.ny));
-                const int kk = int(c / nxy);
-                const uint8_t t = wall_or_out(s, i, j, kk) ? SOLID : (v[k] > 0 ? FLUID : AIR);
-                s.type[c] = t;
-                if (t != FLUID) {
-                    s.pressure[c] = 0.0f;
-                    if (s.x2) {
-                        s.x2[c] = make_float2(0.0f, 0.0f);
-                        s.x64[c] = 0.0;
-                    }
+            const uint32_t o = uint32_t(k) * 256 + threadIdx.x;
+            const uint32_t c = cbase + o;
+            if (c >= s.nc) continue;
+            s.start[c] = sv[slot(o)];
+            s.count[c] = 0;
+            if (vk[k] > kPackedMaxPerCell) atomicOr(&s.chunk[(s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK], 1u);
+            const int i = int(c % uint32_t(s.nx));
+            const int j = int((c / uint32_t(s.nx)) % uint32_t(s.ny));
+            const int kk = int(c / nxy);
+            const uint8_t t = wall_or_out(s, i, j, kk) ? SOLID : (vk[k] > 0 ? FLUID : AIR);
+            s.type[c] = t;
+            if (t != FLUID) {
+                s.pressure[c] = 0.0f;
+                if (s.x2) {
+                    s.x2[c] = make_float2(0.0f, 0.0f);
+                    s.x64[c] = 0.0;
                 }
             }
         }
