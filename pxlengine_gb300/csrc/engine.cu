@@ -514,7 +514,7 @@ cudaError_t BatchImpl::record_gs(cudaStream_t st) {
 
 int BatchImpl::record_post_solve(cudaStream_t st) {
     cudaError_t e;
-    if ((e = launch_project(w_faces, st)) != cudaSuccess) return cuda_fail(e, "project");
+    if ((e = launch_project(w_cells, st)) != cudaSuccess) return cuda_fail(e, "project");
     if ((e = launch_g2p(w_parts, st)) != cudaSuccess) return cuda_fail(e, "g2p");
     return PXF_OK;
 }
@@ -534,7 +534,7 @@ int BatchImpl::record_pre(cudaStream_t st) {
 int BatchImpl::record_post(cudaStream_t st) {
     cudaError_t e;
     if (any_pcg && (e = launch_pcg_finish(pw, st)) != cudaSuccess) return cuda_fail(e, "pcg finish");
-    if ((e = launch_project(w_faces, st)) != cudaSuccess) return cuda_fail(e, "project");
+    if ((e = launch_project(w_cells, st)) != cudaSuccess) return cuda_fail(e, "project");
     if ((e = launch_g2p(w_parts, st)) != cudaSuccess) return cuda_fail(e, "g2p");
     return PXF_OK;
 }
@@ -881,7 +881,7 @@ int BatchImpl::run_eager(KernelTimer* timer, pxf_tune_result* tune) {
         if (timer) timer->segment(200.0);
         if ((e = launch_pcg_finish(pw, stream)) != cudaSuccess) return cuda_fail(e, "pcg finish");
     }
-    if ((e = launch_project(w_faces, stream)) != cudaSuccess) return cuda_fail(e, "project");
+    if ((e = launch_project(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "project");
     if ((e = launch_g2p(w_parts, stream)) != cudaSuccess) return cuda_fail(e, "g2p");
     int rc = wait();
     if (rc) return rc;

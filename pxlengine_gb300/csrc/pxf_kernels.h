@@ -43,7 +43,7 @@ cudaError_t launch_bin(const StageWork& parts, cudaStream_t st);
 cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, cudaStream_t st);
 cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st);
 cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st);
-cudaError_t launch_project(const StageWork& faces, cudaStream_t st);
+cudaError_t launch_project(const StageWork& cells, cudaStream_t st);   // one thread per cell
 cudaError_t launch_g2p(const StageWork& parts, cudaStream_t st);
 
 cudaError_t launch_gather_aos(const SimDev& s, float4* out, cudaStream_t st);

@@ -481,40 +481,53 @@ __global__ void __launch_bounds__(256) k_pressure_rb(Work w, uint32_t parity, ui
 // ------------------------------------------------------------------ project
 // fluid.slang:184-197. With the precision solver the pressure difference comes from the FP64
 // solution.
+// One thread per cell: the u, v and w faces on the cell's low side (and, in the last cell of a
+// row, column or layer, the face on its high side, which touches the outside and becomes 0).
+// Every face is updated once with the reference's arithmetic; consecutive threads touch
+// consecutive cells and faces.
+__device__ __forceinline__ void project_face(const SimDev& s, uint32_t id, int c, int fx, int fy, int fz) {
+    int lo[3] = {fx, fy, fz};
+    lo[c] -= 1;
+    if (wall_or_out(s, lo[0], lo[1], lo[2]) || wall_or_out(s, fx, fy, fz)) {
+        s.vel[id] = 0.0f;
+        return;
+    }
+    const uint32_t nx = uint32_t(s.nx), ny = uint32_t(s.ny);
+    const uint32_t cb = uint32_t(fx) + nx * (uint32_t(fy) + ny * uint32_t(fz));
+    const uint32_t ca = uint32_t(lo[0]) + nx * (uint32_t(lo[1]) + ny * uint32_t(lo[2]));
+    const uint8_t ta = s.type[ca], tb = s.type[cb];
+    if (ta == FLUID || tb == FLUID) {
+        float dp;
+        if (s.solver == 0) {
+            const float pa = ta == FLUID ? s.pressure[ca] : 0.0f;
+            const float pb = tb == FLUID ? s.pressure[cb] : 0.0f;
+            dp = pb - pa;
+        } else {
+            const double pa = ta == FLUID ? s.x64[ca] : 0.0;
+            const double pb = tb == FLUID ? s.x64[cb] : 0.0;
+            dp = float(pb - pa);
+        }
+        s.vel[id] -= s.dt * s.inv_h * dp;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_project(Work w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
-        const SimDev s = w.sims[si];
-        const uint32_t id = (item - w.base[si]) * 256 + threadIdx.x;
-        if (id >= s.nf) continue;
-        uint32_t c, r, dx, dy;
-        if (id < s.nu) { c = 0; r = id; dx = s.nx + 1; dy = s.ny; }
-        else if (id < s.nu + s.nv) { c = 1; r = id - s.nu; dx = s.nx; dy = s.ny + 1; }
-        else { c = 2; r = id - s.nu - s.nv; dx = s.nx; dy = s.ny; }
-        const int fx = int(r % dx), fy = int((r / dx) % dy), fz = int(r / (dx * dy));
-        int lo[3] = {fx, fy, fz};
-        lo[c] -= 1;
-        if (wall_or_out(s, lo[0], lo[1], lo[2]) || wall_or_out(s, fx, fy, fz)) {
-            s.vel[id] = 0.0f;
-            continue;
-        }
-        const uint32_t nx = uint32_t(s.nx), ny = uint32_t(s.ny);
-        const uint32_t cb = uint32_t(fx) + nx * (uint32_t(fy) + ny * uint32_t(fz));
-        const uint32_t ca = uint32_t(lo[0]) + nx * (uint32_t(lo[1]) + ny * uint32_t(lo[2]));
-        const uint8_t ta = s.type[ca], tb = s.type[cb];
-        if (ta == FLUID || tb == FLUID) {
-            float dp;
-            if (s.solver == 0) {
-                const float pa = ta == FLUID ? s.pressure[ca] : 0.0f;
-                const float pb = tb == FLUID ? s.pressure[cb] : 0.0f;
-                dp = pb - pa;
-            } else {
-                const double pa = ta == FLUID ? s.x64[ca] : 0.0;
-                const double pb = tb == FLUID ? s.x64[cb] : 0.0;
-                dp = float(pb - pa);
-            }
-            s.vel[id] -= s.dt * s.inv_h * dp;
-        }
+        const SimDev& s = w.sims[si];
+        const uint32_t c = (item - w.base[si]) * 256 + threadIdx.x;
+        if (c >= s.nc) continue;
+        const uint32_t nx = uint32_t(s.nx), ny = uint32_t(s.ny), nz = uint32_t(s.nz);
+        const int i = int(c % nx), j = int((c / nx) % ny), k = int(c / (nx * ny));
+        const uint32_t fu = uint32_t(i) + (nx + 1) * (uint32_t(j) + ny * uint32_t(k));
+        const uint32_t fv = s.nu + uint32_t(i) + nx * (uint32_t(j) + (ny + 1) * uint32_t(k));
+        const uint32_t fw = s.nu + s.nv + c;
+        project_face(s, fu, 0, i, j, k);
+        project_face(s, fv, 1, i, j, k);
+        project_face(s, fw, 2, i, j, k);
+        if (uint32_t(i) == nx - 1) project_face(s, fu + 1, 0, i + 1, j, k);
+        if (uint32_t(j) == ny - 1) project_face(s, fv + nx, 1, i, j + 1, k);
+        if (uint32_t(k) == nz - 1) project_face(s, fw + nx * ny, 2, i, j, k + 1);
     }
 }
 
@@ -788,8 +801,8 @@ cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uin
     return cudaGetLastError();
 }
 
-cudaError_t launch_project(const StageWork& faces, cudaStream_t st) {
-    k_project<<<grid_for(faces.total, 8), 256, 0, st>>>(mk(faces)); note_launch("k_project", st);
+cudaError_t launch_project(const StageWork& cells, cudaStream_t st) {
+    k_project<<<grid_for(cells.total, 8), 256, 0, st>>>(mk(cells)); note_launch("k_project", st);
     return cudaGetLastError();
 }
 
