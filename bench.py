@@ -269,6 +269,33 @@ def fp64_check(sim, cfg):
             "divergence_linf_dt": divergence_linf(sim), "fp64_rtol": 1e-10}
 
 
+# The reference's example scene's liquid (examples/dam-break.json: 64 x 38 x 32 grid, 139,200
+# particles, 8 substeps of red-black GS with 80 iterations per frame at 24 fps).
+DAM_BREAK_SCENE = ('{"version":1,"nodes":[{"type":"camera"}],"fluids":[{"name":"water",'
+                   '"bounds":[[-1,0,-0.5],[1,1.2,0.5]],"resolution":64,'
+                   '"fill":[{"min":[-0.97,0.03,-0.47],"max":[-0.35,0.95,0.47]}],"substeps":8,"flip":0.95}]}')
+
+
+def reference_scene_frames(P, frames=24):
+    """Device time per frame of the example scene's liquid: 8 substeps plus the surface mesh (the
+    reference publishes about 12 ms per frame for simulation, surface nets and BLAS on a laptop
+    RTX 4080, docs/ROADMAP.md:83)."""
+    with P.FluidState.from_json(DAM_BREAK_SCENE) as s:
+        s.step_timed(16)
+        s.surface_mesh()
+        sim_ms, mesh_ms, tris = 0.0, 0.0, 0
+        for _ in range(frames):
+            sim_ms += s.step_timed(8)
+            m = s.surface_mesh()
+            mesh_ms += m["device_ms"]
+            tris = len(m["indices"])
+        return {"particles": s.particle_count(), "grid": list(s.dims), "frames": frames,
+                "sim_ms_per_frame": sim_ms / frames, "mesh_ms_per_frame": mesh_ms / frames,
+                "ms_per_frame": (sim_ms + mesh_ms) / frames, "triangles": tris,
+                "reference_published_ms_per_frame": 12.0,
+                "reference_hardware": "RTX 4080 Laptop (simulation, surface nets and BLAS per frame)"}
+
+
 def pct(xs, q):
     import numpy as np
     return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if len(xs) else None
@@ -574,6 +601,10 @@ def main():
                    "triangles": int(m["indices"].shape[0]), "overflow": m["overflow"],
                    "surface_cells": list(info["dims"])}
 
+    scene = None
+    if rank == 0 and not args.no_profile:
+        scene = reference_scene_frames(P)
+
     precision = None
     if cfg["solver"] == "pcg" and rank == 0:
         precision = {"divergence_linf_dt": divergence_linf(sim)}
@@ -601,6 +632,7 @@ def main():
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": (launches_per_substep * args.steps) if launches_per_substep else None,
                 "solver": solver_stats, "precision": precision, "kernels": kernels, "surface_mesh": surface,
+                "reference_scene": scene,
                 "wall_s_timed": t_wall}
         print(json.dumps(line), flush=True)
     sim.close()
