@@ -1202,6 +1202,12 @@ __global__ void __launch_bounds__(THREADS) k_pcg_ctl(const SimDev* sims, int n_s
     }
 }
 
+// The same control step without a conditional handle (host-driven loop): no handle-setting
+// code in the graph, which kernel profilers require.
+__global__ void __launch_bounds__(THREADS) k_pcg_ctl_plain(const SimDev* sims, int n_sims, int phase) {
+    ph_ctl(sims, n_sims, phase);
+}
+
 __global__ void k_pcg_cond(const SimDev* sims, int n_sims, cudaGraphConditionalHandle h) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     cudaGraphSetConditional(h, any_active(sims, n_sims) ? 1u : 0u);
@@ -1556,7 +1562,8 @@ static void launch_dep(const char* name, void (*k)(KArgs...), unsigned grid, uns
 
 static cudaError_t ctl(const PcgWork& pw, int phase, cudaStream_t st, cudaGraphConditionalHandle h = 0,
                        uint32_t* ticket = nullptr) {
-    launch_dep("k_pcg_ctl", k_pcg_ctl, pw.n_sims, THREADS, 0, st, pw.sims, pw.n_sims, phase, h, ticket);
+    if (ticket) launch_dep("k_pcg_ctl", k_pcg_ctl, pw.n_sims, THREADS, 0, st, pw.sims, pw.n_sims, phase, h, ticket);
+    else launch_dep("k_pcg_ctl", k_pcg_ctl_plain, pw.n_sims, THREADS, 0, st, pw.sims, pw.n_sims, phase);
     return cudaGetLastError();
 }
 

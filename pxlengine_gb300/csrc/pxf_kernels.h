@@ -39,8 +39,19 @@ constexpr int kMaxP2GShapes = 8;   // capacity of per-shape tables (kNumP2GShape
 cudaError_t launch_scan(const StageWork& chunks, const SimDev* sims, int n_sims, cudaStream_t st);
 cudaError_t launch_scatter(const StageWork& parts, cudaStream_t st);
 cudaError_t launch_bin(const StageWork& parts, cudaStream_t st);
-// lanes: 1 = strided lane mapping over a tile's cells, 0 = blocked.
-cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, cudaStream_t st);
+// Heaviest-first processing order of a stage's P2G tiles, rebuilt every substep from the
+// counting sort's cell starts: tiles go into log2 buckets of the particle count of their own
+// cells (bucket = count leading zeros, 0 = heaviest, 32 = empty), so the blocks of the densest
+// tiles start first and the light ones fill in behind them.
+constexpr int kOrderBuckets = 33;
+struct TileOrder {
+    uint32_t* order = nullptr;    // [tiles] k-th tile to process
+    uint32_t* bucket = nullptr;   // [tiles] bucket of every tile
+    uint32_t* hist = nullptr;     // [2 * kOrderBuckets] bucket sizes, then placement cursors (zeroed first)
+};
+cudaError_t launch_tile_order(const StageWork& tiles, int shape, const TileOrder& o, cudaStream_t st);
+// lanes: 1 = strided lane mapping over a tile's particles, 0 = blocked; order: null = item order.
+cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, const uint32_t* order, cudaStream_t st);
 cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st);
 cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st);
 cudaError_t launch_project(const StageWork& cells, cudaStream_t st);   // one thread per cell

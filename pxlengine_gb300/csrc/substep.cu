@@ -258,32 +258,44 @@ struct P2GTile {
     static constexpr int FW = TX * TY * (TZ + 1);
     static constexpr int NF = FU + FV + FW;
     static constexpr int SMEM = NF * 2 * 4;
+    static constexpr int NR = (TY + 2) * (TZ + 2);   // x-rows of the tile and its halo
+    static_assert(NR <= 128, "the row scan uses the block's first four warps");
 };
 
 template <int TX, int TY, int TZ, bool PACKED>
 __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc, int* __restrict__ swac,
                                          unsigned long long* __restrict__ spk, const int org[3], const int E[3][3],
-                                         bool strided) {
+                                         bool strided, const uint32_t* __restrict__ s_rb,
+                                         const uint32_t* __restrict__ s_rs) {
     using T = P2GTile<TX, TY, TZ>;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int x0 = org[0], y0 = org[1], z0 = org[2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int sbase[3] = {0, T::FU, T::FU + T::FV};
     const float SW = 65536.0f;
-    const int rows_y = TY + 2;
-    const int nrows = (TY + 2) * (TZ + 2);
-    for (int r = warp; r < nrows; r += blockDim.x >> 5) {
-        const int yy = y0 - 1 + r % rows_y, zz = z0 - 1 + r / rows_y;
-        if (yy < 0 || yy >= s.ny || zz < 0 || zz >= s.nz) continue;
-        const int xa = max(x0 - 1, 0), xb = min(x0 + TX, s.nx - 1);
-        const uint32_t rowc = uint32_t(s.nx) * (uint32_t(yy) + uint32_t(s.ny) * uint32_t(zz));
-        const uint32_t pb = s.start[rowc + xa], pe = s.start[rowc + xb + 1];
-        // strided: each lane takes a contiguous slice of the row, so at any step the lanes of a
-        // warp sit in different cells and rarely hit the same face; otherwise lanes take
-        // consecutive particles (coalesced loads).
-        const uint32_t per = (pe - pb + 31) / 32;
-        for (uint32_t t = 0; t < per; t++) {
-            const uint32_t j = strided ? pb + lane * per + t : pb + t * 32 + lane;
-            if (j >= pe) continue;
+    // The tile's rows (its cells plus the one-cell halo, x-rows of the sorted particle array)
+    // concatenated: list position q of row r is s_rs[r] + (q - s_rb[r]). Each warp takes an equal
+    // slice of the list, so a dense row spreads over all warps instead of holding one back.
+    // strided: each lane takes a contiguous part of the slice, so at any step the lanes of a warp
+    // sit in different cells and rarely hit the same face; otherwise lanes take consecutive
+    // particles (coalesced loads).
+    const uint32_t total = s_rb[T::NR];
+    const uint32_t qa = uint32_t(uint64_t(total) * uint32_t(warp) / uint32_t(nw));
+    const uint32_t qb = uint32_t(uint64_t(total) * uint32_t(warp + 1) / uint32_t(nw));
+    const uint32_t per = (qb - qa + 31) / 32;
+    uint32_t q = strided ? qa + uint32_t(lane) * per : qa + uint32_t(lane);
+    const uint32_t qend = strided ? min(q + per, qb) : qb;
+    const uint32_t step = strided ? 1u : 32u;
+    int r = 0;
+    {
+        int hi = T::NR;   // largest r with s_rb[r] <= q
+        while (hi - r > 1) {
+            const int mid = (r + hi) >> 1;
+            if (s_rb[mid] <= q) r = mid; else hi = mid;
+        }
+    }
+    for (; q < qend; q += step) {
+        while (s_rb[r + 1] <= q) r++;
+        const uint32_t j = s_rs[r] + (q - s_rb[r]);
+        {
             const float4 P = s.posB[j];
             const float4 V = s.velB[j];
             const float x[3] = {P.x, P.y, P.z};
@@ -336,13 +348,16 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
 }
 
 template <int TX, int TY, int TZ>
-__global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack) {
+__global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack, const uint32_t* __restrict__ order) {
     using T = P2GTile<TX, TY, TZ>;
     extern __shared__ unsigned long long smem64[];
+    __shared__ uint32_t s_rb[T::NR + 1], s_rs[T::NR], s_wt[4];
     unsigned long long* spk = smem64;
     int* sacc = reinterpret_cast<int*>(smem64);
     int* swac = sacc + T::NF;
-    for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t k = blockIdx.x; k < w.total; k += gridDim.x) {
+        const uint32_t item = order ? __ldg(order + k) : k;
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         const uint32_t t = item - w.base[si];
@@ -350,6 +365,36 @@ __global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack) {
         const int x0 = int(t % uint32_t(ntx)) * TX;
         const int y0 = int((t / uint32_t(ntx)) % uint32_t(nty)) * TY;
         const int z0 = int(t / uint32_t(ntx * nty)) * TZ;
+        // Particle range of every row and the rows' offsets in the concatenated list (a scan
+        // over the first four warps).
+        uint32_t len = 0;
+        if (threadIdx.x < T::NR) {
+            const int yy = y0 - 1 + int(threadIdx.x) % (TY + 2), zz = z0 - 1 + int(threadIdx.x) / (TY + 2);
+            uint32_t pb = 0;
+            if (yy >= 0 && yy < s.ny && zz >= 0 && zz < s.nz) {
+                const int xa = max(x0 - 1, 0), xb = min(x0 + TX, s.nx - 1);
+                const uint32_t rowc = uint32_t(s.nx) * (uint32_t(yy) + uint32_t(s.ny) * uint32_t(zz));
+                pb = s.start[rowc + xa];
+                len = s.start[rowc + xb + 1] - pb;
+            }
+            s_rs[threadIdx.x] = pb;
+        }
+        uint32_t inc = len;
+        if (threadIdx.x < 128) {
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if (lane == 31) s_wt[warp] = inc;
+        }
+        __syncthreads();
+        if (threadIdx.x < T::NR) {
+            uint32_t pre = 0;
+            for (int k2 = 0; k2 < warp; k2++) pre += s_wt[k2];
+            s_rb[threadIdx.x + 1] = pre + inc;
+            if (threadIdx.x == 0) s_rb[0] = 0;
+        }
         const int n[3] = {s.nx, s.ny, s.nz};
         const int org[3] = {x0, y0, z0};
         const int TT[3] = {TX, TY, TZ};
@@ -369,8 +414,8 @@ __global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack) {
         const bool packed = pack && __ldg(s.chunk + (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK) == 0;
         for (int i = threadIdx.x; i < T::NF; i += blockDim.x) spk[i] = 0ull;   // also zeroes sacc / swac
         __syncthreads();
-        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E, strided != 0);
-        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E, strided != 0);
+        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E, strided != 0, s_rb, s_rs);
+        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E, strided != 0, s_rb, s_rs);
         __syncthreads();
 
         // Epilogue: normalize + forces for the owned faces.
@@ -406,6 +451,67 @@ __global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack) {
         }
         __syncthreads();
     }
+}
+
+// ------------------------------------------------------------------ P2G tile order
+// Bucket of every tile (leading zeros of its own cells' particle count) and the bucket sizes.
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(256) k_tile_weigh(Work w, uint32_t* __restrict__ bucket, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kOrderBuckets];
+    for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item < w.total) {
+        const int si = find_sim(w, item);
+        const SimDev& s = w.sims[si];
+        const int nx = s.nx, ny = s.ny, nz = s.nz;
+        const uint32_t* __restrict__ start = s.start;
+        const uint32_t t = item - w.base[si];
+        const int ntx = (nx + TX - 1) / TX, nty = (ny + TY - 1) / TY;
+        const int x0 = int(t % uint32_t(ntx)) * TX;
+        const int y0 = int((t / uint32_t(ntx)) % uint32_t(nty)) * TY;
+        const int z0 = int(t / uint32_t(ntx * nty)) * TZ;
+        const int x1 = min(x0 + TX, nx), y1 = min(y0 + TY, ny), z1 = min(z0 + TZ, nz);
+        uint32_t weight = 0;
+        for (int z = z0; z < z1; z++)
+            for (int y = y0; y < y1; y++) {
+                const uint32_t rowc = uint32_t(nx) * (uint32_t(y) + uint32_t(ny) * uint32_t(z));
+                weight += start[rowc + x1] - start[rowc + x0];
+            }
+        const uint32_t b = uint32_t(__clz(weight));
+        bucket[item] = b;
+        atomicAdd(&sh[b], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// Places every tile after the tiles of the heavier buckets: one global reservation per bucket
+// and block, shared-memory ranks inside the block.
+__global__ void __launch_bounds__(256) k_tile_place(uint32_t total, const uint32_t* __restrict__ bucket,
+                                                    uint32_t* __restrict__ hist, uint32_t* __restrict__ order) {
+    __shared__ uint32_t off[kOrderBuckets], cnt[kOrderBuckets];
+    if (threadIdx.x < kOrderBuckets) cnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        uint32_t a = 0;
+        for (int i = 0; i < kOrderBuckets; i++) {
+            off[i] = a;
+            a += hist[i];
+        }
+    }
+    __syncthreads();
+    const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t b = 0, rank = 0;
+    if (item < total) {
+        b = bucket[item];
+        rank = atomicAdd(&cnt[b], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < kOrderBuckets && cnt[threadIdx.x])
+        off[threadIdx.x] += atomicAdd(&hist[kOrderBuckets + threadIdx.x], cnt[threadIdx.x]);
+    __syncthreads();
+    if (item < total) order[off[b] + rank] = item;
 }
 
 // ------------------------------------------------------------------ divergence
@@ -734,7 +840,7 @@ static inline Work mk(const StageWork& sw) {
 }
 
 template <int TX, int TY, int TZ>
-static cudaError_t launch_p2g_t(const StageWork& sw, int lanes, cudaStream_t st) {
+static cudaError_t launch_p2g_t(const StageWork& sw, int lanes, const uint32_t* order, cudaStream_t st) {
     using T = P2GTile<TX, TY, TZ>;
     static bool attr = false;
     if (!attr) {
@@ -742,14 +848,24 @@ static cudaError_t launch_p2g_t(const StageWork& sw, int lanes, cudaStream_t st)
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_p2g<TX, TY, TZ>, 256, T::SMEM);
-    if (per_sm < 1) per_sm = 1;
     static const int pack = [] { const char* v = std::getenv("PXF_P2G_PACKED"); return v ? std::atoi(v) : 0; }();
     // One block per tile: tiles of the liquid hold most of the work and those of the air none, so
-    // the block scheduler's dynamic assignment balances the SMs (a grid-strided loop would not).
-    (void)per_sm;
-    k_p2g<TX, TY, TZ><<<sw.total ? sw.total : 1u, 256, T::SMEM, st>>>(mk(sw), lanes, pack); note_launch("k_p2g", st);
+    // the block scheduler's dynamic assignment (heaviest tiles first with an order) balances the
+    // SMs (a grid-strided loop would not).
+    k_p2g<TX, TY, TZ><<<sw.total ? sw.total : 1u, 256, T::SMEM, st>>>(mk(sw), lanes, pack, order);
+    note_launch("k_p2g", st);
+    return cudaGetLastError();
+}
+
+template <int TX, int TY, int TZ>
+static cudaError_t launch_tile_order_t(const StageWork& sw, const TileOrder& o, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(o.hist, 0, 2 * kOrderBuckets * sizeof(uint32_t), st);
+    if (e != cudaSuccess || sw.total == 0) return e;
+    const uint32_t blocks = (sw.total + 255) / 256;
+    k_tile_weigh<TX, TY, TZ><<<blocks, 256, 0, st>>>(mk(sw), o.bucket, o.hist);
+    note_launch("k_tile_weigh", st);
+    k_tile_place<<<blocks, 256, 0, st>>>(sw.total, o.bucket, o.hist, o.order);
+    note_launch("k_tile_place", st);
     return cudaGetLastError();
 }
 
@@ -764,13 +880,23 @@ void p2g_shape(int shape, int out[3]) {
     out[2] = kP2GShapes[shape][2];
 }
 
-cudaError_t launch_p2g(const StageWork& sw, int shape, int lanes, cudaStream_t st) {
+cudaError_t launch_p2g(const StageWork& sw, int shape, int lanes, const uint32_t* order, cudaStream_t st) {
     switch (shape) {
-        case 1: return launch_p2g_t<32, 4, 4>(sw, lanes, st);
-        case 2: return launch_p2g_t<16, 8, 8>(sw, lanes, st);
-        case 3: return launch_p2g_t<64, 4, 4>(sw, lanes, st);
-        case 4: return launch_p2g_t<16, 4, 4>(sw, lanes, st);
-        default: return launch_p2g_t<32, 8, 8>(sw, lanes, st);
+        case 1: return launch_p2g_t<32, 4, 4>(sw, lanes, order, st);
+        case 2: return launch_p2g_t<16, 8, 8>(sw, lanes, order, st);
+        case 3: return launch_p2g_t<64, 4, 4>(sw, lanes, order, st);
+        case 4: return launch_p2g_t<16, 4, 4>(sw, lanes, order, st);
+        default: return launch_p2g_t<32, 8, 8>(sw, lanes, order, st);
+    }
+}
+
+cudaError_t launch_tile_order(const StageWork& sw, int shape, const TileOrder& o, cudaStream_t st) {
+    switch (shape) {
+        case 1: return launch_tile_order_t<32, 4, 4>(sw, o, st);
+        case 2: return launch_tile_order_t<16, 8, 8>(sw, o, st);
+        case 3: return launch_tile_order_t<64, 4, 4>(sw, o, st);
+        case 4: return launch_tile_order_t<16, 4, 4>(sw, o, st);
+        default: return launch_tile_order_t<32, 8, 8>(sw, o, st);
     }
 }
 

@@ -72,6 +72,24 @@ def test_thirty_substeps_bit_exact(lib):
         particles_equal(s, o)
 
 
+def _random_state(s, pile):
+    n = s.particle_count()
+    nx, ny, nz = s.dims
+    h = np.float32(s.cell)
+    rng = np.random.default_rng(1234)
+    p = np.zeros((n, 8), dtype=np.float32)
+    lo = h * np.float32(1.001)
+    hi = h * (np.array([nx, ny, nz], dtype=np.float32) - np.float32(1.001))
+    p[:, :3] = (lo + rng.random((n, 3), dtype=np.float32) * (hi - lo)).astype(np.float32)
+    k = n // 4
+    p[:k, :3] = (rng.integers(1, [nx - 1, ny - 1, nz - 1], size=(k, 3)).astype(np.float32) * h)
+    p[k:k + pile, :3] = np.float32(5.5) * h           # a pile of particles in one cell
+    p[:, 4:7] = rng.normal(0, 2.0, (n, 3)).astype(np.float32)
+    p[:50, 4:7] *= np.float32(50.0)
+    s.write_particles(p)
+    return p
+
+
 @pytest.mark.parametrize("pile", [300, 5000])
 def test_random_particles_and_edges(lib, pile):
     """Arbitrary particle states: jittered positions, exact cell-boundary positions, a pile of
@@ -79,20 +97,7 @@ def test_random_particles_and_edges(lib, pile):
     the two-atomic path), velocities of both signs and magnitudes."""
     f = dam(res=24, ppc=2) if pile < 1000 else dam(res=32, ppc=8)
     with P.FluidState(f, fps=24.0, seed=1, options=P.make_options(keep_p2g_sums=True)) as s:
-        n = s.particle_count()
-        nx, ny, nz = s.dims
-        h = np.float32(s.cell)
-        rng = np.random.default_rng(1234)
-        p = np.zeros((n, 8), dtype=np.float32)
-        lo = h * np.float32(1.001)
-        hi = h * (np.array([nx, ny, nz], dtype=np.float32) - np.float32(1.001))
-        p[:, :3] = (lo + rng.random((n, 3), dtype=np.float32) * (hi - lo)).astype(np.float32)
-        k = n // 4
-        p[:k, :3] = (rng.integers(1, [nx - 1, ny - 1, nz - 1], size=(k, 3)).astype(np.float32) * h)
-        p[k:k + pile, :3] = np.float32(5.5) * h           # a pile of particles in one cell
-        p[:, 4:7] = rng.normal(0, 2.0, (n, 3)).astype(np.float32)
-        p[:50, 4:7] *= np.float32(50.0)
-        s.write_particles(p)
+        p = _random_state(s, pile)
         np.testing.assert_array_equal(s.read_particles(), p * np.array([1, 1, 1, 0, 1, 1, 1, 0], np.float32))
         o = oracle_for(s, f)
         s.step(1)
@@ -103,6 +108,28 @@ def test_random_particles_and_edges(lib, pile):
         o.step(3)
         grids_equal(s, o)
         particles_equal(s, o)
+
+
+@pytest.mark.parametrize("order", ["1", "0"])
+def test_p2g_variants_on_a_pile(lib, monkeypatch, order):
+    """Every P2G tile shape and lane mapping, with the heaviest-first tile order or in index
+    order, gives the oracle's integer sums on a random state with a 5000-particle pile in one
+    cell."""
+    monkeypatch.setenv("PXF_P2G_ORDER", order)
+    f = dam(res=32, ppc=8)
+    ref = None
+    for lanes in ("0", "1"):
+        monkeypatch.setenv("PXF_P2G_STRIDED", lanes)
+        for shape in range(5):
+            opts = P.make_options(keep_p2g_sums=True, p2g_tile=shape)
+            with P.FluidState(f, fps=24.0, seed=1, options=opts) as s:
+                _random_state(s, 5000)
+                if ref is None:
+                    ref = oracle_for(s, f)
+                    ref.step(1)
+                s.step(1)
+                grids_equal(s, ref, acc=True)
+                particles_equal(s, ref)
 
 
 def test_run_to_run_determinism(lib):
