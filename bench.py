@@ -171,7 +171,8 @@ def kernel_bytes(kernel, N, F, C, Cf, lv=None):
         "k_p2g": 32 * N + 8 * F + 4 * C,             # sorted particles and cell starts in; vel, vel_old out
         "k_divergence": 4 * F + 1 * C + 4 * C + 2 * C,   # faces, flags in; divergence, neighbour record out
         "k_pressure_rb": 8 * C,                      # one colour: 16C per red-black iteration
-        "k_pressure_rb_list": 8 * C,                 # the same sweep over the system-cell lists
+        "k_pressure_rb_list": 9 * Cf,                # one colour of the system cells: list, record, div in,
+                                                     # p out (14 B per colour cell), other colour's p in
         "k_pcg_dir": 22 * Cf,                        # list, z, p, record in; p', Ap out
         "k_pcg_update": 38 * Cf,                     # list, p, Ap, r, x (8 B) in; r, x, red z out
         "k_project": 8 * F + 5 * C,                  # faces in and out; pressure, flags in
@@ -181,8 +182,9 @@ def kernel_bytes(kernel, N, F, C, Cf, lv=None):
 
 def substep_bytes(N, F, C, Cf, solver, iters):
     """Algorithmic bytes of one substep: 96N + 60F + 40C plus the pressure solve (red-black GS:
-    16C per iteration; PCG: 56 B per system cell per iteration)."""
-    press = 16 * C * iters if solver == "gs" else 56 * Cf * iters
+    18 B per system cell per iteration, two colour sweeps over the system cells; PCG: 56 B per
+    system cell per iteration)."""
+    press = 18 * Cf * iters if solver == "gs" else 56 * Cf * iters
     return 96 * N + 60 * F + 40 * C + press
 
 

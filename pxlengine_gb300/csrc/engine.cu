@@ -73,6 +73,13 @@ struct BatchImpl {
     size_t cap_tile = 0;
     TileOrder ord;                       // heaviest-first P2G tile order (rebuilt every substep)
     size_t cap_order = 0;
+    bool auto_shape = false;             // tile shape picked every substep (p2g_pick_small)
+    bool p2g_if_ok = true;               // the automatic pick as two IF nodes in captured graphs
+    TileOrder ord_big;                   // buckets and order of the 32x8x8 tiles (the pick's input)
+    size_t cap_order_big = 0;
+    uint32_t fair = 0;                   // particles per P2G block slot (the pick's threshold)
+    bool pick_dynamic = false;           // fair share large enough for the 32x8x8 tiles to win
+    uint32_t* d_pick = nullptr;          // last pick (1: small tiles)
     uint16_t* d_sim_of = nullptr;        // item -> simulation tables of every stage
     size_t cap_sim_of = 0;
     uint32_t* d_act = nullptr;           // compacted item lists of the CG loop's stages
@@ -108,6 +115,9 @@ struct BatchImpl {
     int record_post_solve(cudaStream_t st);  // project, g2p
     cudaError_t record_gs(cudaStream_t st);  // the red-black sweeps
     cudaError_t p2g(int shape, int lanes, cudaStream_t st);   // tile order + P2G of a tile shape
+    int record_p2g(cudaStream_t st);                          // P2G of the substep (automatic shape)
+    cudaError_t p2g_branch(int shape, cudaStream_t st);
+    cudaError_t capture_if(cudaStream_t st, cudaGraphConditionalHandle h);
     int step(uint32_t n);
     int wait();
     void drop_graphs();
@@ -257,6 +267,10 @@ BatchImpl::~BatchImpl() {
     if (ord.order) cudaFree(ord.order);
     if (ord.bucket) cudaFree(ord.bucket);
     if (ord.hist) cudaFree(ord.hist);
+    if (ord_big.order) cudaFree(ord_big.order);
+    if (ord_big.bucket) cudaFree(ord_big.bucket);
+    if (ord_big.hist) cudaFree(ord_big.hist);
+    if (d_pick) cudaFree(d_pick);
     if (d_sim_of) cudaFree(d_sim_of);
     if (d_act) cudaFree(d_act);
     if (d_act_n) cudaFree(d_act_n);
@@ -304,8 +318,15 @@ int BatchImpl::rebuild() {
     if (!tuned) {
         tile_shape = p2g_shape_index();
         p2g_lanes = p2g_lanes_default();
+        auto_shape = tile_shape < 0;
+        if (auto_shape) tile_shape = kP2GAutoSmall;
         for (pxf_sim* sm : sims)
-            if (sm->opts.p2g_tile >= 0 && sm->opts.p2g_tile < kNumP2GShapes) tile_shape = sm->opts.p2g_tile;
+            if (sm->opts.p2g_tile >= 0 && sm->opts.p2g_tile < kNumP2GShapes) {
+                tile_shape = sm->opts.p2g_tile;
+                auto_shape = false;
+            }
+    } else {
+        auto_shape = false;
     }
     int shape[3];
     p2g_shape(tile_shape, shape);
@@ -412,6 +433,31 @@ int BatchImpl::rebuild() {
     }
     if (!ord.hist && (e = cudaMalloc(&ord.hist, 2 * kOrderBuckets * sizeof(uint32_t))) != cudaSuccess)
         return cuda_fail(e, "tile order");
+    if (w_tiles_s[kP2GAutoBig].total > cap_order_big) {
+        if (ord_big.order) cudaFree(ord_big.order);
+        if (ord_big.bucket) cudaFree(ord_big.bucket);
+        ord_big.order = ord_big.bucket = nullptr;
+        cap_order_big = std::max<size_t>(w_tiles_s[kP2GAutoBig].total, 2 * cap_order_big);
+        if ((e = cudaMalloc(&ord_big.order, cap_order_big * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "tile order");
+        if ((e = cudaMalloc(&ord_big.bucket, cap_order_big * sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "tile order");
+    }
+    if (!ord_big.hist && (e = cudaMalloc(&ord_big.hist, 2 * kOrderBuckets * sizeof(uint32_t))) != cudaSuccess)
+        return cuda_fail(e, "tile order");
+    if (!d_pick) {
+        if ((e = cudaMalloc(&d_pick, sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "tile pick");
+        if ((e = cudaMemsetAsync(d_pick, 0, sizeof(uint32_t), stream)) != cudaSuccess) return cuda_fail(e, "tile pick");
+    }
+    {
+        uint64_t np_all = 0;
+        for (pxf_sim* sm : sims) np_all += sm->dev.np;
+        const char* fv = std::getenv("PXF_P2G_FAIR");   // threshold override (tests)
+        const uint64_t f = fv ? std::strtoull(fv, nullptr, 10) : np_all / std::max<uint32_t>(p2g_slots(kP2GAutoBig), 1u);
+        fair = uint32_t(std::min<uint64_t>(f, 0xffffffffull));
+        // Below 65536 particles per slot the pick chooses the small tiles as soon as FLIP packs a
+        // tile to 32 particles per cell, and both shapes run about equally before that: the
+        // small tiles are used without a per-substep pick.
+        pick_dynamic = fv != nullptr || fair >= 65536u;
+    }
     pw.sims = d_sims;
     pw.n_sims = n;
     pw.chunks = w_lchunks;
@@ -510,7 +556,7 @@ int BatchImpl::record_gs_part(cudaStream_t st) {
     cudaError_t e;
     if ((e = launch_scan(w_chunks, d_sims, n, st)) != cudaSuccess) return cuda_fail(e, "scan");
     if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
-    if ((e = p2g(tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+    if (int rc = record_p2g(st)) return rc;
     if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
     if (any_gs && (e = record_gs(st)) != cudaSuccess) return cuda_fail(e, "pressure");
     return PXF_OK;
@@ -546,12 +592,94 @@ cudaError_t BatchImpl::p2g(int shape, int lanes, cudaStream_t st) {
     return launch_p2g(w_tiles_s[shape], shape, lanes, ordered ? ord.order : nullptr, st);
 }
 
+// The automatic pick as one IF/ELSE node (condition set by k_p2g_pick): the 32x8x8 P2G, else
+// the 32x4x4 P2G; both bodies captured on the side stream.
+cudaError_t BatchImpl::capture_if(cudaStream_t st, cudaGraphConditionalHandle h) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+    alignas(cudaGraphNodeParams) unsigned char np_raw[sizeof(cudaGraphNodeParams)];
+    std::memset(np_raw, 0, sizeof(np_raw));
+    cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_raw);
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 2;   // [0]: condition set, [1]: else
+        e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+    }
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    for (int branch = 0; branch < 2 && e == cudaSuccess; branch++) {
+        cudaGraph_t body = np.conditional.phGraph_out[branch];
+        e = cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e1 = p2g_branch(branch == 0 ? kP2GAutoBig : kP2GAutoSmall, side);
+            cudaGraph_t out = body;
+            cudaError_t e2 = cudaStreamEndCapture(side, &out);
+            e = e1 != cudaSuccess ? e1 : e2;
+        }
+    }
+    return e;
+}
+
+// P2G of one shape of the automatic pick: placement of its tiles (buckets from the pair pass),
+// then the P2G in that heaviest-first order.
+cudaError_t BatchImpl::p2g_branch(int shape, cudaStream_t st) {
+    const TileOrder& o = shape == kP2GAutoBig ? ord_big : ord;
+    cudaError_t e = launch_tile_place(w_tiles_s[shape], o, st);
+    return e != cudaSuccess ? e : launch_p2g(w_tiles_s[shape], shape, p2g_lanes, o.order, st);
+}
+
+// P2G of one substep. With the automatic shape: the buckets of both shapes, then the pick —
+// inside a capture an IF/ELSE node whose condition k_p2g_pick sets, eagerly a read-back of the
+// buckets (captures without conditional nodes use the small tiles).
+int BatchImpl::record_p2g(cudaStream_t st) {
+    cudaError_t e;
+    if (!auto_shape || !pick_dynamic) {
+        if ((e = p2g(tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+        return PXF_OK;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if ((e = cudaStreamIsCapturing(st, &cs)) != cudaSuccess) return cuda_fail(e, "p2g");
+    const bool capturing = cs == cudaStreamCaptureStatusActive;
+    static const bool no_cond = [] { const char* v = std::getenv("PXF_NO_COND_GRAPH"); return v && v[0] == '1'; }();
+    if ((e = launch_tile_weigh_pair(w_tiles_s[kP2GAutoBig], w_tiles_s[kP2GAutoSmall], ord_big, ord, st)) != cudaSuccess)
+        return cuda_fail(e, "tile weigh");
+    if (capturing && (!p2g_if_ok || no_cond || !cond_ok)) {
+        if ((e = p2g_branch(kP2GAutoSmall, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+        return PXF_OK;
+    }
+    if (capturing) {
+        cudaGraph_t cg = nullptr;
+        cudaGraphConditionalHandle h = 0;
+        e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, nullptr, nullptr, nullptr);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, 0);
+        if (e == cudaSuccess) e = launch_p2g_pick(ord_big.hist, fair, h, d_pick, st);
+        if (e == cudaSuccess) e = capture_if(st, h);
+        if (e != cudaSuccess) {
+            p2g_if_ok = false;    // the capture fails; the next one uses the small tiles throughout
+            return cuda_fail(e, "p2g pick");
+        }
+        return PXF_OK;
+    }
+    uint32_t hist[2 * kOrderBuckets];
+    if ((e = cudaMemcpyAsync(hist, ord_big.hist, sizeof(hist), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return cuda_fail(e, "tile weigh");
+    if (int rc = wait()) return rc;
+    if ((e = p2g_branch(p2g_pick_small(hist, fair) ? kP2GAutoSmall : kP2GAutoBig, st)) != cudaSuccess)
+        return cuda_fail(e, "p2g");
+    return PXF_OK;
+}
+
 int BatchImpl::record_pre(cudaStream_t st) {
     const int n = int(sims.size());
     cudaError_t e;
     if ((e = launch_scan(w_chunks, d_sims, n, st)) != cudaSuccess) return cuda_fail(e, "scan");
     if ((e = launch_scatter(w_parts, st)) != cudaSuccess) return cuda_fail(e, "scatter");
-    if ((e = p2g(tile_shape, p2g_lanes, st)) != cudaSuccess) return cuda_fail(e, "p2g");
+    if (int rc = record_p2g(st)) return rc;
     if ((e = launch_divergence(w_cells, st)) != cudaSuccess) return cuda_fail(e, "divergence");
     if (any_gs && (e = record_gs(st)) != cudaSuccess) return cuda_fail(e, "pressure");
     if (any_pcg && (e = launch_pcg_init(pw, st)) != cudaSuccess) return cuda_fail(e, "pcg init");
@@ -619,6 +747,7 @@ int BatchImpl::capture() {
     // (one launch, grid barriers between phases; slower on one large simulation).
     const char* persist_env = std::getenv("PXF_PCG_PERSISTENT");
     const bool want_persist = persist_env && persist_env[0] == '1';
+    const bool had_p2g_if = p2g_if_ok;
     if (any_pcg && persist_ok && want_persist && persist_grid > 0) {
         if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
             return cuda_fail(e, "begin capture");
@@ -634,6 +763,7 @@ int BatchImpl::capture() {
         }
         if (ex) cudaGraphExecDestroy(ex);
         cudaGetLastError();
+        if (rc && had_p2g_if && !p2g_if_ok) return capture();   // once more without the P2G IF nodes
         if (rc) return rc;
         persist_ok = false;   // fall back to the graph-of-kernels loop
     }
@@ -705,6 +835,7 @@ int BatchImpl::capture() {
         }
         if (ex) cudaGraphExecDestroy(ex);
         cudaGetLastError();
+        if (rc && had_p2g_if && !p2g_if_ok) return capture();   // once more without the P2G IF nodes
         if (rc) return rc;
         if (!if_ok && !retried_plain_if) {
             retried_plain_if = true;
@@ -882,8 +1013,8 @@ int BatchImpl::run_eager(KernelTimer* timer, pxf_tune_result* tune) {
         std::snprintf(tune->chosen, sizeof(tune->chosen), "p2g %dx%dx%d %s", sh[0], sh[1], sh[2],
                       p2g_lanes ? "strided" : "blocked");
         dirty = true;    // recapture: later substeps use the chosen variant
-    } else if ((e = p2g(tile_shape, p2g_lanes, stream)) != cudaSuccess) {
-        return cuda_fail(e, "p2g");
+    } else if (int rc = record_p2g(stream)) {
+        return rc;
     }
     if ((e = launch_divergence(w_cells, stream)) != cudaSuccess) return cuda_fail(e, "divergence");
     if (any_gs && (e = record_gs(stream)) != cudaSuccess) return cuda_fail(e, "pressure");
@@ -991,14 +1122,13 @@ int p2g_lanes_default() {
     return v ? (std::atoi(v) ? 1 : 0) : 1;
 }
 
-// Default tile shape 32x4x4 (index 1): with the heaviest-first order it stays fastest or close
-// to it from the seeded state through the settled dam break, where FLIP packs cells with
-// thousands of particles (PXF_P2G_TILE overrides, read per recording).
+// P2G tile shape: -1 (default) picks 32x8x8 or 32x4x4 every substep from the particle
+// distribution (p2g_pick_small); PXF_P2G_TILE=<index> fixes one shape (read per recording).
 int p2g_shape_index() {
     const char* env = std::getenv("PXF_P2G_TILE");
-    int shape = env ? std::atoi(env) : 1;
-    if (shape < 0 || shape >= kNumP2GShapes) shape = 1;
-    return shape;
+    if (!env) return -1;
+    const int shape = std::atoi(env);
+    return shape >= 0 && shape < kNumP2GShapes ? shape : -1;
 }
 
 }  // namespace pxf

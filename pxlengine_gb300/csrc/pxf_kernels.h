@@ -50,8 +50,34 @@ struct TileOrder {
     uint32_t* hist = nullptr;     // [2 * kOrderBuckets] bucket sizes, then placement cursors (zeroed first)
 };
 cudaError_t launch_tile_order(const StageWork& tiles, int shape, const TileOrder& o, cudaStream_t st);
+cudaError_t launch_tile_weigh(const StageWork& tiles, int shape, const TileOrder& o, cudaStream_t st);   // buckets only
+cudaError_t launch_tile_place(const StageWork& tiles, const TileOrder& o, cudaStream_t st);            // order from buckets
+// Buckets of the 32x8x8 tiles (big) and of the 32x4x4 tiles (small) in one pass (the automatic pick).
+cudaError_t launch_tile_weigh_pair(const StageWork& big, const StageWork& small, const TileOrder& ob,
+                                  const TileOrder& os, cudaStream_t st);
+
+// Automatic P2G tile shape: the large 32x8x8 tiles (least halo work) unless the heaviest one
+// holds more particles than a fair share of the GPU's P2G block slots (FLIP packs cells with
+// thousands of particles as a splash settles: that tile would outlast the others), then 32x4x4.
+// The heaviest tile is taken at the lower end of its bucket (2^(31 - bucket) particles).
+constexpr int kP2GAutoBig = 0, kP2GAutoSmall = 1;
+__host__ __device__ inline bool p2g_small_for_bucket(int heaviest_bucket, uint32_t fair) {
+    const uint32_t heaviest = heaviest_bucket >= 32 ? 0u : (1u << (31 - heaviest_bucket));
+    return heaviest > fair;
+}
+inline bool p2g_pick_small(const uint32_t* hist, uint32_t fair) {
+    int b = 0;
+    while (b < kOrderBuckets - 1 && hist[b] == 0) b++;
+    return p2g_small_for_bucket(b, fair);
+}
+uint32_t p2g_slots(int shape);   // resident P2G blocks of a tile shape on the whole GPU
+// Sets the IF/ELSE condition of the P2G branches from the 32x8x8 buckets (graph capture only):
+// 1 = large tiles, 0 = small; pick (nullable) receives 1 when the small tiles were chosen.
+cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, uint32_t* pick,
+                            cudaStream_t st);
 // lanes: 1 = strided lane mapping over a tile's particles, 0 = blocked; order: null = item order.
 cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, const uint32_t* order, cudaStream_t st);
+
 cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st);
 cudaError_t launch_pressure_rb(const StageWork& half_cells, uint32_t parity, uint32_t it, cudaStream_t st);
 cudaError_t launch_project(const StageWork& cells, cudaStream_t st);   // one thread per cell

@@ -16,6 +16,7 @@
 #include "pxf_device.cuh"
 #include "pxf_kernels.h"
 
+#include <algorithm>
 #include <cstdlib>
 
 namespace pxf {
@@ -292,9 +293,14 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
             if (s_rb[mid] <= q) r = mid; else hi = mid;
         }
     }
+    uint32_t row_end = s_rb[r + 1], row_off = s_rs[r] - s_rb[r];
     for (; q < qend; q += step) {
-        while (s_rb[r + 1] <= q) r++;
-        const uint32_t j = s_rs[r] + (q - s_rb[r]);
+        while (q >= row_end) {
+            r++;
+            row_end = s_rb[r + 1];
+            row_off = s_rs[r] - s_rb[r];
+        }
+        const uint32_t j = q + row_off;
         {
             const float4 P = s.posB[j];
             const float4 V = s.velB[j];
@@ -348,6 +354,7 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
 }
 
 template <int TX, int TY, int TZ>
+// order: null = item order; otherwise the k-th block takes tile order[k].
 __global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack, const uint32_t* __restrict__ order) {
     using T = P2GTile<TX, TY, TZ>;
     extern __shared__ unsigned long long smem64[];
@@ -454,13 +461,15 @@ __global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack, cons
 }
 
 // ------------------------------------------------------------------ P2G tile order
-// Bucket of every tile (leading zeros of its own cells' particle count) and the bucket sizes.
+// Bucket of every tile (leading zeros of its own cells' particle count) and the bucket sizes:
+// one warp per tile, lanes over the tile's x-rows.
 template <int TX, int TY, int TZ>
 __global__ void __launch_bounds__(256) k_tile_weigh(Work w, uint32_t* __restrict__ bucket, uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[kOrderBuckets];
     for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x) sh[i] = 0;
     __syncthreads();
-    const uint32_t item = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const uint32_t item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (item < w.total) {
         const int si = find_sim(w, item);
         const SimDev& s = w.sims[si];
@@ -471,20 +480,84 @@ __global__ void __launch_bounds__(256) k_tile_weigh(Work w, uint32_t* __restrict
         const int x0 = int(t % uint32_t(ntx)) * TX;
         const int y0 = int((t / uint32_t(ntx)) % uint32_t(nty)) * TY;
         const int z0 = int(t / uint32_t(ntx * nty)) * TZ;
-        const int x1 = min(x0 + TX, nx), y1 = min(y0 + TY, ny), z1 = min(z0 + TZ, nz);
+        const int x1 = min(x0 + TX, nx);
         uint32_t weight = 0;
-        for (int z = z0; z < z1; z++)
-            for (int y = y0; y < y1; y++) {
+        for (int r = lane; r < TY * TZ; r += 32) {
+            const int y = y0 + r % TY, z = z0 + r / TY;
+            if (y < ny && z < nz) {
                 const uint32_t rowc = uint32_t(nx) * (uint32_t(y) + uint32_t(ny) * uint32_t(z));
-                weight += start[rowc + x1] - start[rowc + x0];
+                weight += __ldg(start + rowc + x1) - __ldg(start + rowc + x0);
             }
-        const uint32_t b = uint32_t(__clz(weight));
-        bucket[item] = b;
-        atomicAdd(&sh[b], 1u);
+        }
+        weight = __reduce_add_sync(0xffffffffu, weight);
+        if (lane == 0) {
+            const uint32_t b = uint32_t(__clz(weight));
+            bucket[item] = b;
+            atomicAdd(&sh[b], 1u);
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x)
         if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+// Buckets of the 32x8x8 tiles and of the four 32x4x4 tiles inside each, for the automatic
+// shape pick: one warp per large tile, two x-rows per lane, a sum per quarter.
+__global__ void __launch_bounds__(256) k_tile_weigh_pair(Work big, Work small, uint32_t* __restrict__ bucket_big,
+                                                         uint32_t* __restrict__ hist_big,
+                                                         uint32_t* __restrict__ bucket_small,
+                                                         uint32_t* __restrict__ hist_small) {
+    __shared__ uint32_t shb[kOrderBuckets], shs[kOrderBuckets];
+    for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x) shb[i] = shs[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const uint32_t item = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (item < big.total) {
+        const int si = find_sim(big, item);
+        const SimDev& s = big.sims[si];
+        const int nx = s.nx, ny = s.ny, nz = s.nz;
+        const uint32_t* __restrict__ start = s.start;
+        const uint32_t t = item - big.base[si];
+        const uint32_t ntx = uint32_t((nx + 31) / 32), pty = uint32_t((ny + 7) / 8);
+        const uint32_t px = t % ntx, py = (t / ntx) % pty, pz = t / (ntx * pty);
+        const int x0 = int(px) * 32, x1 = min(x0 + 32, nx);
+        uint32_t q[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int r = lane + 32 * h;              // row r: y offset r % 8, z offset r / 8
+            const int y = int(py) * 8 + (r & 7), z = int(pz) * 8 + (r >> 3);
+            uint32_t wr = 0;
+            if (y < ny && z < nz) {
+                const uint32_t rowc = uint32_t(nx) * (uint32_t(y) + uint32_t(ny) * uint32_t(z));
+                wr = __ldg(start + rowc + x1) - __ldg(start + rowc + x0);
+            }
+            const int quarter = ((r & 7) >= 4 ? 1 : 0) + ((r >> 3) >= 4 ? 2 : 0);
+#pragma unroll
+            for (int k = 0; k < 4; k++) q[k] += quarter == k ? wr : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) q[k] = __reduce_add_sync(0xffffffffu, q[k]);
+        if (lane == 0) {
+            const uint32_t b = uint32_t(__clz(q[0] + q[1] + q[2] + q[3]));
+            bucket_big[item] = b;
+            atomicAdd(&shb[b], 1u);
+        }
+        if (lane < 4) {
+            const uint32_t sy = 2u * py + uint32_t(lane & 1), sz = 2u * pz + uint32_t(lane >> 1);
+            const uint32_t nty = uint32_t((ny + 3) / 4), ntz = uint32_t((nz + 3) / 4);
+            if (sy < nty && sz < ntz) {
+                const uint32_t wq = lane == 0 ? q[0] : lane == 1 ? q[1] : lane == 2 ? q[2] : q[3];
+                const uint32_t b = uint32_t(__clz(wq));
+                bucket_small[small.base[si] + px + ntx * (sy + nty * sz)] = b;
+                atomicAdd(&shs[b], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kOrderBuckets; i += blockDim.x) {
+        if (shb[i]) atomicAdd(&hist_big[i], shb[i]);
+        if (shs[i]) atomicAdd(&hist_small[i], shs[i]);
+    }
 }
 
 // Places every tile after the tiles of the heavier buckets: one global reservation per bucket
@@ -492,12 +565,17 @@ __global__ void __launch_bounds__(256) k_tile_weigh(Work w, uint32_t* __restrict
 __global__ void __launch_bounds__(256) k_tile_place(uint32_t total, const uint32_t* __restrict__ bucket,
                                                     uint32_t* __restrict__ hist, uint32_t* __restrict__ order) {
     __shared__ uint32_t off[kOrderBuckets], cnt[kOrderBuckets];
-    if (threadIdx.x < kOrderBuckets) cnt[threadIdx.x] = 0;
+    if (threadIdx.x < kOrderBuckets) {
+        cnt[threadIdx.x] = 0;
+        off[threadIdx.x] = hist[threadIdx.x];
+    }
+    __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t a = 0;
         for (int i = 0; i < kOrderBuckets; i++) {
+            const uint32_t c = off[i];
             off[i] = a;
-            a += hist[i];
+            a += c;
         }
     }
     __syncthreads();
@@ -858,15 +936,19 @@ static cudaError_t launch_p2g_t(const StageWork& sw, int lanes, const uint32_t* 
 }
 
 template <int TX, int TY, int TZ>
-static cudaError_t launch_tile_order_t(const StageWork& sw, const TileOrder& o, cudaStream_t st) {
+static cudaError_t launch_tile_weigh_t(const StageWork& sw, const TileOrder& o, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(o.hist, 0, 2 * kOrderBuckets * sizeof(uint32_t), st);
     if (e != cudaSuccess || sw.total == 0) return e;
-    const uint32_t blocks = (sw.total + 255) / 256;
-    k_tile_weigh<TX, TY, TZ><<<blocks, 256, 0, st>>>(mk(sw), o.bucket, o.hist);
+    k_tile_weigh<TX, TY, TZ><<<(sw.total + 7) / 8, 256, 0, st>>>(mk(sw), o.bucket, o.hist);
     note_launch("k_tile_weigh", st);
-    k_tile_place<<<blocks, 256, 0, st>>>(sw.total, o.bucket, o.hist, o.order);
-    note_launch("k_tile_place", st);
     return cudaGetLastError();
+}
+
+template <int TX, int TY, int TZ>
+static uint32_t p2g_slots_t() {
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_p2g<TX, TY, TZ>, 256, P2GTile<TX, TY, TZ>::SMEM);
+    return uint32_t(std::max(per_sm, 1)) * uint32_t(std::max(sm_count(), 1));
 }
 
 const int kP2GShapes[][3] = {{32, 8, 8}, {32, 4, 4}, {16, 8, 8}, {64, 4, 4}, {16, 4, 4}};
@@ -890,14 +972,64 @@ cudaError_t launch_p2g(const StageWork& sw, int shape, int lanes, const uint32_t
     }
 }
 
-cudaError_t launch_tile_order(const StageWork& sw, int shape, const TileOrder& o, cudaStream_t st) {
+
+cudaError_t launch_tile_weigh(const StageWork& sw, int shape, const TileOrder& o, cudaStream_t st) {
     switch (shape) {
-        case 1: return launch_tile_order_t<32, 4, 4>(sw, o, st);
-        case 2: return launch_tile_order_t<16, 8, 8>(sw, o, st);
-        case 3: return launch_tile_order_t<64, 4, 4>(sw, o, st);
-        case 4: return launch_tile_order_t<16, 4, 4>(sw, o, st);
-        default: return launch_tile_order_t<32, 8, 8>(sw, o, st);
+        case 1: return launch_tile_weigh_t<32, 4, 4>(sw, o, st);
+        case 2: return launch_tile_weigh_t<16, 8, 8>(sw, o, st);
+        case 3: return launch_tile_weigh_t<64, 4, 4>(sw, o, st);
+        case 4: return launch_tile_weigh_t<16, 4, 4>(sw, o, st);
+        default: return launch_tile_weigh_t<32, 8, 8>(sw, o, st);
     }
+}
+
+cudaError_t launch_tile_place(const StageWork& sw, const TileOrder& o, cudaStream_t st) {
+    if (sw.total == 0) return cudaSuccess;
+    k_tile_place<<<(sw.total + 255) / 256, 256, 0, st>>>(sw.total, o.bucket, o.hist, o.order);
+    note_launch("k_tile_place", st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_weigh_pair(const StageWork& big, const StageWork& small, const TileOrder& ob,
+                                  const TileOrder& os, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(ob.hist, 0, 2 * kOrderBuckets * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(os.hist, 0, 2 * kOrderBuckets * sizeof(uint32_t), st);
+    if (e != cudaSuccess || big.total == 0) return e;
+    k_tile_weigh_pair<<<(big.total + 7) / 8, 256, 0, st>>>(mk(big), mk(small), ob.bucket, ob.hist, os.bucket, os.hist);
+    note_launch("k_tile_weigh", st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_order(const StageWork& sw, int shape, const TileOrder& o, cudaStream_t st) {
+    cudaError_t e = launch_tile_weigh(sw, shape, o, st);
+    return e != cudaSuccess ? e : launch_tile_place(sw, o, st);
+}
+
+uint32_t p2g_slots(int shape) {
+    switch (shape) {
+        case 1: return p2g_slots_t<32, 4, 4>();
+        case 2: return p2g_slots_t<16, 8, 8>();
+        case 3: return p2g_slots_t<64, 4, 4>();
+        case 4: return p2g_slots_t<16, 4, 4>();
+        default: return p2g_slots_t<32, 8, 8>();
+    }
+}
+
+__global__ void k_p2g_pick(const uint32_t* __restrict__ hist, uint32_t fair, cudaGraphConditionalHandle h,
+                           uint32_t* pick) {
+    // one warp: the heaviest non-empty bucket (buckets 0..31 by lane; none of them: empty tiles)
+    const unsigned nonempty = __ballot_sync(0xffffffffu, hist[threadIdx.x] != 0u);
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const bool small = p2g_small_for_bucket(nonempty ? __ffs(nonempty) - 1 : 32, fair);
+    cudaGraphSetConditional(h, small ? 0u : 1u);
+    if (pick) *pick = small ? 1u : 0u;
+}
+
+cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, uint32_t* pick,
+                            cudaStream_t st) {
+    k_p2g_pick<<<1, 32, 0, st>>>(hist, fair, h, pick);
+    note_launch("k_p2g_pick", st);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_scan(const StageWork& chunks, const SimDev* sims, int n_sims, cudaStream_t st) {

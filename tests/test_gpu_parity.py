@@ -132,6 +132,25 @@ def test_p2g_variants_on_a_pile(lib, monkeypatch, order):
                 particles_equal(s, ref)
 
 
+@pytest.mark.parametrize("fair", ["0", "4294967295"])
+def test_p2g_automatic_shape_branches(lib, monkeypatch, fair):
+    """The automatic P2G tile shape is two IF nodes in the substep graph whose conditions a
+    kernel sets from the 32x8x8 tile buckets (eager substeps read the buckets back). Forcing
+    the small tiles (threshold 0) or the large ones (no threshold) gives the oracle's bits over
+    graph and eager substeps of a random state with a pile."""
+    monkeypatch.delenv("PXF_P2G_TILE", raising=False)
+    monkeypatch.setenv("PXF_P2G_FAIR", fair)
+    f = dam(res=32, ppc=8)
+    with P.FluidState(f, fps=24.0, seed=1, options=P.make_options(keep_p2g_sums=True)) as s:
+        _random_state(s, 5000)
+        o = oracle_for(s, f)
+        s.step(2)
+        s.profile_substep()
+        o.step(3)
+        grids_equal(s, o, acc=True)
+        particles_equal(s, o)
+
+
 def test_run_to_run_determinism(lib):
     f = dam(res=48, ppc=8, iters=40)
     out = []
