@@ -583,13 +583,22 @@ int BatchImpl::record_post_solve(cudaStream_t st) {
     return PXF_OK;
 }
 
+// Work split inside a P2G block (lane-mapping bit 1): whole x-rows per warp (the picked large
+// tiles: uniformly dense states) or equal slices of the tile's concatenated rows (default);
+// PXF_P2G_ROWS=0/1 (read per recording) forces one.
+static int p2g_rows(bool dflt) {
+    const char* v = std::getenv("PXF_P2G_ROWS");
+    const bool rows = v ? v[0] == '1' : dflt;
+    return rows ? 2 : 0;
+}
+
 // PXF_P2G_ORDER=0 (read per recording) processes the tiles in index order.
 cudaError_t BatchImpl::p2g(int shape, int lanes, cudaStream_t st) {
     const char* v = std::getenv("PXF_P2G_ORDER");
     const bool ordered = !(v && v[0] == '0');
     cudaError_t e;
     if (ordered && (e = launch_tile_order(w_tiles_s[shape], shape, ord, st)) != cudaSuccess) return e;
-    return launch_p2g(w_tiles_s[shape], shape, lanes, ordered ? ord.order : nullptr, st);
+    return launch_p2g(w_tiles_s[shape], shape, lanes | p2g_rows(false), ordered ? ord.order : nullptr, st);
 }
 
 // The automatic pick as one IF/ELSE node (condition set by k_p2g_pick): the 32x8x8 P2G, else
@@ -630,7 +639,7 @@ cudaError_t BatchImpl::capture_if(cudaStream_t st, cudaGraphConditionalHandle h)
 cudaError_t BatchImpl::p2g_branch(int shape, cudaStream_t st) {
     const TileOrder& o = shape == kP2GAutoBig ? ord_big : ord;
     cudaError_t e = launch_tile_place(w_tiles_s[shape], o, st);
-    return e != cudaSuccess ? e : launch_p2g(w_tiles_s[shape], shape, p2g_lanes, o.order, st);
+    return e != cudaSuccess ? e : launch_p2g(w_tiles_s[shape], shape, p2g_lanes | p2g_rows(shape == kP2GAutoBig), o.order, st);
 }
 
 // P2G of one substep. With the automatic shape: the buckets of both shapes, then the pick —

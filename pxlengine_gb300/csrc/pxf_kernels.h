@@ -75,7 +75,8 @@ uint32_t p2g_slots(int shape);   // resident P2G blocks of a tile shape on the w
 // 1 = large tiles, 0 = small; pick (nullable) receives 1 when the small tiles were chosen.
 cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, uint32_t* pick,
                             cudaStream_t st);
-// lanes: 1 = strided lane mapping over a tile's particles, 0 = blocked; order: null = item order.
+// lanes: bit 0 = strided lane mapping over a tile's particles (else blocked), bit 1 = whole x-rows
+// per warp (else equal slices of the tile's particle list); order: null = item order.
 cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, const uint32_t* order, cudaStream_t st);
 
 cudaError_t launch_divergence(const StageWork& cells, cudaStream_t st);

@@ -266,41 +266,14 @@ struct P2GTile {
 template <int TX, int TY, int TZ, bool PACKED>
 __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc, int* __restrict__ swac,
                                          unsigned long long* __restrict__ spk, const int org[3], const int E[3][3],
-                                         bool strided, const uint32_t* __restrict__ s_rb,
+                                         bool strided, bool by_rows, const uint32_t* __restrict__ s_rb,
                                          const uint32_t* __restrict__ s_rs) {
     using T = P2GTile<TX, TY, TZ>;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int sbase[3] = {0, T::FU, T::FU + T::FV};
     const float SW = 65536.0f;
-    // The tile's rows (its cells plus the one-cell halo, x-rows of the sorted particle array)
-    // concatenated: list position q of row r is s_rs[r] + (q - s_rb[r]). Each warp takes an equal
-    // slice of the list, so a dense row spreads over all warps instead of holding one back.
-    // strided: each lane takes a contiguous part of the slice, so at any step the lanes of a warp
-    // sit in different cells and rarely hit the same face; otherwise lanes take consecutive
-    // particles (coalesced loads).
-    const uint32_t total = s_rb[T::NR];
-    const uint32_t qa = uint32_t(uint64_t(total) * uint32_t(warp) / uint32_t(nw));
-    const uint32_t qb = uint32_t(uint64_t(total) * uint32_t(warp + 1) / uint32_t(nw));
-    const uint32_t per = (qb - qa + 31) / 32;
-    uint32_t q = strided ? qa + uint32_t(lane) * per : qa + uint32_t(lane);
-    const uint32_t qend = strided ? min(q + per, qb) : qb;
-    const uint32_t step = strided ? 1u : 32u;
-    int r = 0;
-    {
-        int hi = T::NR;   // largest r with s_rb[r] <= q
-        while (hi - r > 1) {
-            const int mid = (r + hi) >> 1;
-            if (s_rb[mid] <= q) r = mid; else hi = mid;
-        }
-    }
-    uint32_t row_end = s_rb[r + 1], row_off = s_rs[r] - s_rb[r];
-    for (; q < qend; q += step) {
-        while (q >= row_end) {
-            r++;
-            row_end = s_rb[r + 1];
-            row_off = s_rs[r] - s_rb[r];
-        }
-        const uint32_t j = q + row_off;
+    // The 24 fixed-point face terms of particle j, added to the owned faces in shared memory.
+    auto particle = [&](uint32_t j) {
         {
             const float4 P = s.posB[j];
             const float4 V = s.velB[j];
@@ -320,8 +293,12 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
                     if (a == c) gq += 0.5f;
                     const int b = f2i(floorf(gq));
                     const float f = gq - float(b);
-                    wt[a][0] = fmix(1.0f - f, f, 0.0f);
-                    wt[a][1] = fmix(1.0f - f, f, 1.0f);
+                    // fmix(1 - f, f, 0) and fmix(1 - f, f, 1) (fluid.slang's lerp weights) equal
+                    // 1 - f and f for every finite f up to the sign of a zero, which the integer
+                    // terms drop, and both forms are NaN for a NaN f; an infinite f comes from an
+                    // infinite position, whose saturated cell index owns no face of any tile.
+                    wt[a][0] = 1.0f - f;
+                    wt[a][1] = f;
                     lb[a] = b - org[a];
                     ok[a][0] = unsigned(lb[a]) < unsigned(E[c][a]);
                     ok[a][1] = unsigned(lb[a] + 1) < unsigned(E[c][a]);
@@ -350,12 +327,54 @@ __device__ __forceinline__ void p2g_tile(const SimDev& s, int* __restrict__ sacc
                 }
             }
         }
+    };
+    // The tile's rows (its cells plus the one-cell halo, x-rows of the sorted particle array)
+    // concatenated: list position q of row r is s_rs[r] + (q - s_rb[r]).
+    // strided: each lane takes a contiguous part of its warp's share, so at any step the lanes of
+    // a warp sit in different cells and rarely hit the same face; otherwise lanes take
+    // consecutive particles (coalesced loads).
+    if (by_rows) {
+        // whole rows per warp (uniformly dense tiles)
+        for (int rr = warp; rr < T::NR; rr += nw) {
+            const uint32_t pb = s_rs[rr], n = s_rb[rr + 1] - s_rb[rr];
+            const uint32_t per = (n + 31) / 32;
+            for (uint32_t t = 0; t < per; t++) {
+                const uint32_t o = strided ? uint32_t(lane) * per + t : t * 32 + uint32_t(lane);
+                if (o < n) particle(pb + o);
+            }
+        }
+        return;
+    }
+    // an equal slice of the list per warp, so a dense row spreads over all warps
+    const uint32_t total = s_rb[T::NR];
+    const uint32_t qa = uint32_t(uint64_t(total) * uint32_t(warp) / uint32_t(nw));
+    const uint32_t qb = uint32_t(uint64_t(total) * uint32_t(warp + 1) / uint32_t(nw));
+    const uint32_t per = (qb - qa + 31) / 32;
+    uint32_t q = strided ? qa + uint32_t(lane) * per : qa + uint32_t(lane);
+    const uint32_t qend = strided ? min(q + per, qb) : qb;
+    const uint32_t step = strided ? 1u : 32u;
+    int r = 0;
+    {
+        int hi = T::NR;   // largest r with s_rb[r] <= q
+        while (hi - r > 1) {
+            const int mid = (r + hi) >> 1;
+            if (s_rb[mid] <= q) r = mid; else hi = mid;
+        }
+    }
+    uint32_t row_end = s_rb[r + 1], row_off = s_rs[r] - s_rb[r];
+    for (; q < qend; q += step) {
+        while (q >= row_end) {
+            r++;
+            row_end = s_rb[r + 1];
+            row_off = s_rs[r] - s_rb[r];
+        }
+        particle(q + row_off);
     }
 }
 
-template <int TX, int TY, int TZ>
 // order: null = item order; otherwise the k-th block takes tile order[k].
-__global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack, const uint32_t* __restrict__ order) {
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(256, 3) k_p2g(Work w, int strided, int pack, const uint32_t* __restrict__ order) {
     using T = P2GTile<TX, TY, TZ>;
     extern __shared__ unsigned long long smem64[];
     __shared__ uint32_t s_rb[T::NR + 1], s_rs[T::NR], s_wt[4];
@@ -421,8 +440,8 @@ __global__ void __launch_bounds__(256) k_p2g(Work w, int strided, int pack, cons
         const bool packed = pack && __ldg(s.chunk + (s.nc + SCAN_CHUNK - 1) / SCAN_CHUNK) == 0;
         for (int i = threadIdx.x; i < T::NF; i += blockDim.x) spk[i] = 0ull;   // also zeroes sacc / swac
         __syncthreads();
-        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E, strided != 0, s_rb, s_rs);
-        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E, strided != 0, s_rb, s_rs);
+        if (packed) p2g_tile<TX, TY, TZ, true>(s, sacc, swac, spk, org, E, strided & 1, (strided & 2) != 0, s_rb, s_rs);
+        else p2g_tile<TX, TY, TZ, false>(s, sacc, swac, spk, org, E, strided & 1, (strided & 2) != 0, s_rb, s_rs);
         __syncthreads();
 
         // Epilogue: normalize + forces for the owned faces.
