@@ -789,17 +789,37 @@ __device__ __forceinline__ float gather(const float* __restrict__ buf, const Tap
     return acc;
 }
 
-__global__ void __launch_bounds__(256) k_g2p(Work w) {
+__global__ void __launch_bounds__(256, 4) k_g2p(Work w) {
+    // The particle records of the thread's next item are loaded before the current one is
+    // processed, so their HBM latency overlaps the current gathers.
+    float4 Pn = make_float4(0, 0, 0, 0), Vn = Pn;
+    if (blockIdx.x < w.total) {
+        const int si = find_sim(w, blockIdx.x);
+        const uint32_t i = (blockIdx.x - w.base[si]) * 256 + threadIdx.x;
+        if (i < w.sims[si].np) {
+            Pn = w.sims[si].posB[i];
+            Vn = w.sims[si].velB[i];
+        }
+    }
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
         const SimDev s = w.sims[si];
         const uint32_t i = (item - w.base[si]) * 256 + threadIdx.x;
         const bool live = i < s.np;
         uint32_t cell = 0xffffffffu;
-        float4 P = make_float4(0, 0, 0, 0), V = make_float4(0, 0, 0, 0);
+        float4 P = Pn, V = Vn;
+        {
+            const uint32_t nx_item = item + gridDim.x;
+            if (nx_item < w.total) {
+                const int sn = find_sim(w, nx_item);
+                const uint32_t in = (nx_item - w.base[sn]) * 256 + threadIdx.x;
+                if (in < w.sims[sn].np) {
+                    Pn = w.sims[sn].posB[in];
+                    Vn = w.sims[sn].velB[in];
+                }
+            }
+        }
         if (live) {
-            P = s.posB[i];
-            V = s.velB[i];
             const float* fvel[3] = {s.vel, s.vel + s.nu, s.vel + s.nu + s.nv};
             const float* fold[3] = {s.vel_old, s.vel_old + s.nu, s.vel_old + s.nu + s.nv};
             float pic[3], old[3];
