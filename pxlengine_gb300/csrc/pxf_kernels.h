@@ -113,10 +113,12 @@ constexpr uint32_t kTailCells = 8192;   // the shared-memory tail starts at the 
 static_assert(kTailCells <= 65536, "tail lists hold cell indices as 16-bit values");
 // Shared-memory floats a tail level of nc cells takes: r, z (float), neighbour record and list (u16).
 __host__ __device__ constexpr uint32_t tail_level_floats(uint32_t nc) { return 3 * nc; }
-// List chunks (cells) of the system-cell lists: level 0 (PXF_L0_CHUNK) and the levels below it
+// List chunks (cells) of the system-cell lists: level 0 (PXF_L0_CHUNK; PXF_GS_CHUNK for the
+// red-black GS) and the levels below it
 // (PXF_COARSE_CHUNK); multiples of 256 up to 8192, read once per process.
 uint32_t coarse_chunk();
-uint32_t level0_chunk();
+uint32_t level0_chunk();      // level-0 list chunk of the precision solver
+uint32_t level0_chunk_gs(uint64_t nc);   // level-0 list chunk of the red-black GS on nc cells
 cudaError_t mg_tail_attr(size_t smem);
 
 // Grid barrier of the persistent solve (device memory, zeroed at every launch).
