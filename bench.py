@@ -127,7 +127,7 @@ class ClockSampler:
 # one ncu capture of this workload, keyed by (config, kernel); the capture is summarised in profiles/.
 KERNEL_TRAFFIC = {
     ("dam256", "k_p2g"): 408.48e6,
-    ("dam256", "k_g2p"): 543.80e6,
+    ("dam256", "k_g2p"): 545.89e6,
     ("dam256", "k_pcg_update"): 30.11e6,
     ("dam256_gs", "k_pressure_rb_list"): 12.47e6,
 }
