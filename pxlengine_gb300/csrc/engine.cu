@@ -74,7 +74,7 @@ struct BatchImpl {
     TileOrder ord;                       // heaviest-first P2G tile order (rebuilt every substep)
     size_t cap_order = 0;
     bool auto_shape = false;             // tile shape picked every substep (p2g_pick_small)
-    bool p2g_if_ok = true;               // the automatic pick as two IF nodes in captured graphs
+    bool p2g_if_ok = true;               // the automatic pick as an IF/ELSE node in captured graphs
     TileOrder ord_big;                   // buckets and order of the 32x8x8 tiles (the pick's input)
     size_t cap_order_big = 0;
     uint32_t fair = 0;                   // particles per P2G block slot (the pick's threshold)
@@ -773,7 +773,7 @@ int BatchImpl::capture() {
         }
         if (ex) cudaGraphExecDestroy(ex);
         cudaGetLastError();
-        if (rc && had_p2g_if && !p2g_if_ok) return capture();   // once more without the P2G IF nodes
+        if (rc && had_p2g_if && !p2g_if_ok) return capture();   // once more without the P2G IF/ELSE node
         if (rc) return rc;
         persist_ok = false;   // fall back to the graph-of-kernels loop
     }
@@ -845,7 +845,7 @@ int BatchImpl::capture() {
         }
         if (ex) cudaGraphExecDestroy(ex);
         cudaGetLastError();
-        if (rc && had_p2g_if && !p2g_if_ok) return capture();   // once more without the P2G IF nodes
+        if (rc && had_p2g_if && !p2g_if_ok) return capture();   // once more without the P2G IF/ELSE node
         if (rc) return rc;
         if (!if_ok && !retried_plain_if) {
             retried_plain_if = true;
