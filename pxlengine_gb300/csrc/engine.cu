@@ -1107,17 +1107,18 @@ uint32_t coarse_chunk() {
 }
 
 uint32_t level0_chunk() {
-    static const uint32_t cs = chunk_env("PXF_L0_CHUNK", 4096);
+    static const uint32_t cs = chunk_env("PXF_L0_CHUNK", 5120);
     return cs;
 }
 
 // The red-black GS sweeps one colour per launch with one cell per thread: on grids up to 2^23
-// cells smaller chunks (more blocks) pay (2.00 vs 2.08 ms per substep at 256x128x128), on larger
-// ones the 4096-cell chunks keep the sweeps' block count down (17.5 vs 18.8 ms at 512x256x256).
+// cells smaller chunks (more blocks) pay (2.00 vs 2.08 ms per substep at 256x128x128 with 2048
+// against 4096 cells), on larger ones larger chunks keep the sweeps' block count down (17.0, 17.5
+// and 18.8 ms at 512x256x256 with 6144, 4096 and 2048 cells).
 uint32_t level0_chunk_gs(uint64_t nc) {
     static const uint32_t fixed = chunk_env("PXF_GS_CHUNK", 0);
     if (fixed) return fixed;
-    return nc <= (uint64_t(1) << 23) ? 2048u : 4096u;
+    return nc <= (uint64_t(1) << 23) ? 2048u : 6144u;
 }
 
 bool trace_on() {
