@@ -84,7 +84,9 @@ typedef struct {
     float velocity_sigma;          /* > 0: add N(0, sigma) per velocity component at seeding */
     uint32_t velocity_seed;        /* seed of that jitter */
     double wait_timeout_s;         /* bound on every host wait, default 600 s */
-    int32_t p2g_tile;              /* P2G tile shape index (-1: tuned / default) */
+    int32_t p2g_tile;              /* P2G tile shape index (pxf_tune_result.tile_shape); -1: the
+                                      autotuner's choice, else 32x4x4, or on very large grids a
+                                      per-substep pick between 32x8x8 and 32x4x4 */
     uint32_t pcg_precond;          /* 0: multigrid V-cycle (default), 1: Jacobi */
     uint32_t mg_coarse_iters;      /* red-black iterations on the coarsest multigrid level, default 2 */
     uint32_t mg_smooth_pairs;      /* red-black pairs of pre- and of post-smoothing per level, default 2 */
@@ -195,7 +197,7 @@ PXF_API int pxf_profile_substep(pxf_sim* sim, pxf_stage_time* out, uint32_t cap,
  * writes the same bits, so the substep's result equals a normal substep's; it counts as one. */
 typedef struct {
     int32_t tile_shape;   /* 0: 32x8x8, 1: 32x4x4, 2: 16x8x8, 3: 64x4x4, 4: 16x4x4 cells */
-    int32_t lanes;        /* 1: strided lane mapping over a tile's cells, 0: blocked */
+    int32_t lanes;        /* 1: strided lane mapping over a tile's particles, 0: blocked */
     uint32_t variants;    /* variants timed, in the order shape-major, lanes-minor */
     float ms[16];         /* device time of each variant, ms */
     char chosen[32];
