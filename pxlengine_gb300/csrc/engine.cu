@@ -79,7 +79,6 @@ struct BatchImpl {
     size_t cap_order_big = 0;
     uint32_t fair = 0;                   // particles per P2G block slot (the pick's threshold)
     bool pick_dynamic = false;           // fair share large enough for the 32x8x8 tiles to win
-    uint32_t* d_pick = nullptr;          // last pick (1: small tiles)
     uint16_t* d_sim_of = nullptr;        // item -> simulation tables of every stage
     size_t cap_sim_of = 0;
     uint32_t* d_act = nullptr;           // compacted item lists of the CG loop's stages
@@ -271,7 +270,6 @@ BatchImpl::~BatchImpl() {
     if (ord_big.order) cudaFree(ord_big.order);
     if (ord_big.bucket) cudaFree(ord_big.bucket);
     if (ord_big.hist) cudaFree(ord_big.hist);
-    if (d_pick) cudaFree(d_pick);
     if (d_sim_of) cudaFree(d_sim_of);
     if (d_act) cudaFree(d_act);
     if (d_act_n) cudaFree(d_act_n);
@@ -444,10 +442,6 @@ int BatchImpl::rebuild() {
     }
     if (!ord_big.hist && (e = cudaMalloc(&ord_big.hist, 2 * kOrderBuckets * sizeof(uint32_t))) != cudaSuccess)
         return cuda_fail(e, "tile order");
-    if (!d_pick) {
-        if ((e = cudaMalloc(&d_pick, sizeof(uint32_t))) != cudaSuccess) return cuda_fail(e, "tile pick");
-        if ((e = cudaMemsetAsync(d_pick, 0, sizeof(uint32_t), stream)) != cudaSuccess) return cuda_fail(e, "tile pick");
-    }
     {
         uint64_t np_all = 0;
         for (pxf_sim* sm : sims) np_all += sm->dev.np;
@@ -667,7 +661,7 @@ int BatchImpl::record_p2g(cudaStream_t st) {
         cudaGraphConditionalHandle h = 0;
         e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, nullptr, nullptr, nullptr);
         if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, cg, 0, 0);
-        if (e == cudaSuccess) e = launch_p2g_pick(ord_big.hist, fair, h, d_pick, st);
+        if (e == cudaSuccess) e = launch_p2g_pick(ord_big.hist, fair, h, st);
         if (e == cudaSuccess) e = capture_if(st, h);
         if (e != cudaSuccess) {
             p2g_if_ok = false;    // the capture fails; the next one uses the small tiles throughout

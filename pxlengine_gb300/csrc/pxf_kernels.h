@@ -72,9 +72,8 @@ inline bool p2g_pick_small(const uint32_t* hist, uint32_t fair) {
 }
 uint32_t p2g_slots(int shape);   // resident P2G blocks of a tile shape on the whole GPU
 // Sets the IF/ELSE condition of the P2G branches from the 32x8x8 buckets (graph capture only):
-// 1 = large tiles, 0 = small; pick (nullable) receives 1 when the small tiles were chosen.
-cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, uint32_t* pick,
-                            cudaStream_t st);
+// 1 = large tiles, 0 = small.
+cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, cudaStream_t st);
 // lanes: bit 0 = strided lane mapping over a tile's particles (else blocked), bit 1 = whole x-rows
 // per warp (else equal slices of the tile's particle list); order: null = item order.
 cudaError_t launch_p2g(const StageWork& tiles, int shape, int lanes, const uint32_t* order, cudaStream_t st);

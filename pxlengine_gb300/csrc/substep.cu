@@ -1054,19 +1054,16 @@ uint32_t p2g_slots(int shape) {
     }
 }
 
-__global__ void k_p2g_pick(const uint32_t* __restrict__ hist, uint32_t fair, cudaGraphConditionalHandle h,
-                           uint32_t* pick) {
+__global__ void k_p2g_pick(const uint32_t* __restrict__ hist, uint32_t fair, cudaGraphConditionalHandle h) {
     // one warp: the heaviest non-empty bucket (buckets 0..31 by lane; none of them: empty tiles)
     const unsigned nonempty = __ballot_sync(0xffffffffu, hist[threadIdx.x] != 0u);
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const bool small = p2g_small_for_bucket(nonempty ? __ffs(nonempty) - 1 : 32, fair);
     cudaGraphSetConditional(h, small ? 0u : 1u);
-    if (pick) *pick = small ? 1u : 0u;
 }
 
-cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, uint32_t* pick,
-                            cudaStream_t st) {
-    k_p2g_pick<<<1, 32, 0, st>>>(hist, fair, h, pick);
+cudaError_t launch_p2g_pick(const uint32_t* hist, uint32_t fair, cudaGraphConditionalHandle h, cudaStream_t st) {
+    k_p2g_pick<<<1, 32, 0, st>>>(hist, fair, h);
     note_launch("k_p2g_pick", st);
     return cudaGetLastError();
 }
