@@ -252,11 +252,14 @@ PXF_API void pxf_host_free(void* p);
  * n particle records on the device (d_particles: the [x,y,z,w,vx,vy,vz,w] layout of
  * pxf_read_particles) and an output buffer of C + 1 uint32 on the device (C = dims[0]*dims[1]*dims[2]);
  * d_cell_start receives the exclusive prefix sum of the particles per cell, with the cell of a
- * particle computed as in the substep (clamp(floor((x - origin) / h))) and d_cell_start[C] = n.
+ * particle computed as in the substep: clamp(floor((x - origin) * inv_h)) per axis, where
+ * inv_h = 1.0f / h is rounded to float once and each product is rounded to float; positions
+ * outside the grid land in the nearest boundary cell. d_cell_start[C] = n.
  * The only scratch is a fixed 32 KiB array inside the library on each device that loads it (held
  * until the process exits), so grids are limited to 16,777,216 cells; larger grids return
- * PXF_EINVAL with a message in pxf_last_error(NULL). The first call on each device looks up that
- * array's device address: make it before any stream capture. The work is queued on `stream`
+ * PXF_EINVAL with a message in pxf_last_error(NULL). The first call in each CUDA context (the
+ * context current on the calling thread, else the current device's primary context) looks up
+ * that array's device address in that context: make it before any stream capture. The work is queued on `stream`
  * (a cudaStream_t; NULL = the default stream) and the call returns without waiting. Every call
  * shares the one scratch array, so calls whose work overlaps on the GPU race. */
 PXF_API int pxf_cell_starts_noalloc(const float* d_particles, uint32_t n, const uint32_t dims[3], const float origin[3],

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "../../include/pxlflip.h"
 #include "pxf_device.cuh"
@@ -162,34 +163,84 @@ __global__ void __launch_bounds__(256) k_na_apply(uint32_t* __restrict__ out, ui
     }
 }
 
-// Device address of g_scan_chunks, looked up once per device with that device current.
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
+// Device address of g_scan_chunks in each CUDA context. Every context loads the library's device
+// code on its own, so the address belongs to a context, not to a device ordinal: a caller may
+// have its own (non-primary) context current, or a primary context may have been destroyed and
+// created again. The cache is keyed by the context's process-unique id (cuCtxGetId), reached
+// through the runtime's driver entry points because the library links no libcuda.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
 
-int scratch_for_current_device(void** addr, std::string& err) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+std::mutex g_mu;
+std::unordered_map<unsigned long long, void*> g_scratch_addr;   // context id -> device address
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+
+int driver_entry(const char* name, unsigned version, void** fn, std::string& err) {
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion(name, fn, version, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !*fn) {
+        err = std::string("driver entry point ") + name + " unavailable" +
+              (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : std::string());
+        cudaGetLastError();
         return PXF_ECUDA;
     }
-    if (dev < 0 || dev >= kMaxDevices) {
-        err = "device index out of range";
-        return PXF_EINVAL;
+    return PXF_OK;
+}
+
+int current_context_id(unsigned long long* id, bool* have, std::string& err) {
+    void* ctx = nullptr;
+    if (g_ctx_current(&ctx) != 0) {
+        err = "cuCtxGetCurrent failed";
+        return PXF_ECUDA;
     }
+    *have = ctx != nullptr;
+    if (!ctx) return PXF_OK;
+    if (g_ctx_id(ctx, id) != 0) {
+        err = "cuCtxGetId failed";
+        return PXF_ECUDA;
+    }
+    return PXF_OK;
+}
+
+int scratch_for_current_context(void** addr, std::string& err) {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_scan_chunks);
-        if (e != cudaSuccess || !p) {
-            err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-            cudaGetLastError();
+    if (!g_ctx_current || !g_ctx_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (int rc = driver_entry("cuCtxGetCurrent", 4000, &f1, err)) return rc;
+        if (int rc = driver_entry("cuCtxGetId", 12000, &f2, err)) return rc;
+        g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    unsigned long long id = 0;
+    bool have = false;
+    if (int rc = current_context_id(&id, &have, err)) return rc;
+    if (have) {
+        auto it = g_scratch_addr.find(id);
+        if (it != g_scratch_addr.end()) {
+            *addr = it->second;
+            return PXF_OK;
+        }
+    }
+    // First call in this context (or no context bound yet: the runtime then binds the current
+    // device's primary context while it answers).
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scan_chunks);
+    if (e != cudaSuccess || !p) {
+        err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        return PXF_ECUDA;
+    }
+    if (!have) {
+        if (int rc = current_context_id(&id, &have, err)) return rc;
+        if (!have) {
+            err = "no CUDA context is current after the scratch lookup";
             return PXF_ECUDA;
         }
-        g_scratch_addr[dev] = p;
     }
-    *addr = g_scratch_addr[dev];
+    g_scratch_addr[id] = p;
+    *addr = p;
     return PXF_OK;
 }
 
@@ -218,11 +269,11 @@ int pxf_cell_starts_noalloc(const float* d_particles, uint32_t n, const uint32_t
                                  " cells the fixed scratch of pxf_cell_starts_noalloc supports");
         return PXF_EINVAL;
     }
-    // Set-up on the first call on each device, with that device current: the device address of
-    // the scratch array.
+    // Set-up on the first call in each CUDA context (the context current on the calling thread,
+    // else the current device's primary context): the device address of the scratch array.
     void* scratch = nullptr;
     std::string err;
-    const int rc = scratch_for_current_device(&scratch, err);
+    const int rc = scratch_for_current_context(&scratch, err);
     if (rc != PXF_OK) {
         set_global_error_message(err);
         return rc;
@@ -247,7 +298,8 @@ int pxf_cell_starts_noalloc(const float* d_particles, uint32_t n, const uint32_t
     const unsigned gz = unsigned((nc + 1 + 255) / 256) < cap ? unsigned((nc + 1 + 255) / 256) : cap;
     k_na_zero<<<gz ? gz : 1u, 256, 0, st>>>(d_cell_start, uint32_t(nc + 1));
     if (n) {
-        const unsigned gp = (n + 255) / 256 < cap ? (n + 255) / 256 : cap;
+        const uint64_t blocks = (uint64_t(n) + 255) / 256;   // 64-bit: no wrap for n near 2^32
+        const unsigned gp = blocks < cap ? unsigned(blocks) : cap;
         k_na_count<<<gp, 256, 0, st>>>(g, reinterpret_cast<const float4*>(d_particles), n, d_cell_start);
     }
     const unsigned gc = nchunks < cap ? nchunks : cap;

@@ -44,3 +44,47 @@ def test_cell_starts_noalloc_matches_simulation_binning(lib):
         rc = lib.pxf_cell_starts_noalloc(C.c_void_p(d_parts.data_ptr()), 1, big, origin, C.c_float(s.cell),
                                          C.c_void_p(out.data_ptr()), None)
         assert rc == -1 and "16777216" in lib.pxf_last_error(None).decode()
+
+
+def _host_starts(parts, dims, origin, h):
+    """Exclusive per-cell prefix sum on the host: cell = clamp(floor((x - o) * f32(1/h))) per axis,
+    every step rounded to float32 as on the device."""
+    inv_h = np.float32(1.0) / np.float32(h)
+    idx = []
+    for a in range(3):
+        t = (parts[:, a].astype(np.float32) - np.float32(origin[a])) * inv_h
+        idx.append(np.clip(np.floor(t).astype(np.int64), 0, dims[a] - 1))
+    cell = idx[0] + dims[0] * (idx[1] + dims[1] * idx[2])
+    counts = np.bincount(cell, minlength=int(np.prod(dims)))
+    return np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
+
+
+def test_cell_starts_noalloc_large_grid_and_empty(lib):
+    """A grid above 2^21 cells (more than 1024 scan chunks: the chunk scan carries between its
+    passes), particles partly outside the grid (clamped into the boundary cells), and n = 0."""
+    torch = pytest.importorskip("torch")
+    dims = (256, 128, 128)
+    h = 1.0 / 256
+    origin = (0.0, 0.0, 0.0)
+    rng = np.random.default_rng(5)
+    n = 1_500_000
+    parts = np.zeros((n, 8), dtype=np.float32)
+    ext = np.array([dims[0] * h, dims[1] * h, dims[2] * h], dtype=np.float32)
+    parts[:, :3] = rng.uniform(-0.1, 1.1, (n, 3)).astype(np.float32) * ext
+    want = _host_starts(parts, dims, origin, h)
+    cd = (C.c_uint32 * 3)(*dims)
+    co = (C.c_float * 3)(*origin)
+    out = torch.zeros(int(np.prod(dims)) + 1, dtype=torch.int32, device="cuda")
+    d_parts = torch.from_numpy(parts).to("cuda")
+    for _ in range(2):
+        rc = lib.pxf_cell_starts_noalloc(C.c_void_p(d_parts.data_ptr()), n, cd, co, C.c_float(h),
+                                         C.c_void_p(out.data_ptr()), None)
+        assert rc == 0, lib.pxf_last_error(None).decode()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), want)
+    # n = 0: every start is 0 (the buffer held the previous call's scan)
+    rc = lib.pxf_cell_starts_noalloc(None, 0, cd, co, C.c_float(h), C.c_void_p(out.data_ptr()), None)
+    assert rc == 0, lib.pxf_last_error(None).decode()
+    torch.cuda.synchronize()
+    assert not out.cpu().numpy().any()
+
