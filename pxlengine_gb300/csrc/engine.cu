@@ -62,6 +62,8 @@ struct BatchImpl {
     size_t cap_sims = 0;
     StageWork w_parts, w_tiles, w_cells, w_half, w_faces, w_chunks;
     StageWork w_lchunks;                 // level-0 system-cell list chunks (PCG and the list GS)
+    StageWork w_gsu;                     // units of the streamed red-black GS
+    bool gs_stream = false;              // the red-black GS of this batch is streamed (largest grid)
     PcgWork pw;                          // precision-solver work indexes
     uint32_t max_gs_iters = 0;
     bool any_gs = false, any_pcg = false;
@@ -175,7 +177,7 @@ namespace pxf {
 // Byte layout of one simulation's allocation.
 struct Layout {
     size_t posA, velA, posB, velB, pos0, vel0, vel, vel_old, pressure, div, type, count, start, chunk, info, acc, wacc,
-        x2, x64, r, z, p0, p1, Ap, partial, pcg, total;
+        x2, x64, r, z, p0, p1, Ap, partial, pcg, p_alt, rhs, gs_cnt, gs_flag, total;
     int nlev = 0;
     int dims[kMaxLevels][3];
     size_t ltype[kMaxLevels], linfo[kMaxLevels], lr[kMaxLevels], lz[kMaxLevels], llist[kMaxLevels], llcnt[kMaxLevels];
@@ -194,6 +196,20 @@ static int mg_levels(const uint32_t n[3], int dims[kMaxLevels][3]) {
         L++;
     }
     return L;
+}
+
+// Units of the streamed red-black GS: x-y tiles times z segments.
+static void gs_unit_grid(const uint32_t n[3], uint32_t g[4]) {
+    g[0] = (n[0] + kGsTileX - 1) / kGsTileX;
+    g[1] = (n[1] + kGsTileY - 1) / kGsTileY;
+    g[3] = gs_segment_planes(n[2]);
+    g[2] = (n[2] + g[3] - 1) / g[3];
+}
+
+static uint32_t gs_units(const uint32_t n[3]) {
+    uint32_t g[4];
+    gs_unit_grid(n, g);
+    return g[0] * g[1] * g[2];
 }
 
 static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o) {
@@ -228,6 +244,12 @@ static Layout layout_for(uint32_t np, const uint32_t n[3], const pxf_options& o)
     // level-0 system-cell lists (red then black per chunk): both pressure solvers walk them
     L.llist[0] = take(4 * lchunks * cs0);
     L.llcnt[0] = take(8 * lchunks);
+    if (!pcg) {
+        L.p_alt = take(4 * nc);
+        L.rhs = take(4 * nc);
+        L.gs_cnt = take(nc);
+        L.gs_flag = take(4 * uint64_t(gs_units(n)));
+    }
     if (pcg) {
         L.x2 = take(8 * nc);
         L.x64 = take(8 * nc);
@@ -291,7 +313,7 @@ static inline uint32_t cdiv(uint64_t a, uint64_t b) { return uint32_t((a + b - 1
 
 // Work-index stages: particles, P2G tiles, cells, half cells, faces, 2048-cell chunks, then the
 // multigrid smoothing chunks of each level and the restriction chunks of each level.
-constexpr int kStages = 7 + 3 * kMaxLevels;   // the last: level-0 list chunks
+constexpr int kStages = 8 + 3 * kMaxLevels;   // then streamed-GS units, and last the level-0 list chunks
 
 int BatchImpl::rebuild() {
     cudaError_t e;
@@ -351,6 +373,7 @@ int BatchImpl::rebuild() {
     std::vector<SimDev> host(n);
     std::vector<uint32_t> base(kStages * (n + 1), 0);
     max_gs_iters = 0;
+    uint64_t max_gs_cells = 0;
     any_gs = any_pcg = false;
     pw = PcgWork();
     timeout_s = 0;
@@ -366,6 +389,7 @@ int BatchImpl::rebuild() {
             cdiv(d.nf, kElemItem),
             cdiv(d.nc, kScanChunk)};
         items[kStages - 1] = cdiv(d.nc, d.lev[0].cs);
+        items[kStages - 2] = d.solver == 0 ? d.gs_ntx * d.gs_nty * d.gs_nzs : 0u;
         const bool mg = d.solver == 1 && d.precond == 0;
         for (int l = 0; l < kMaxLevels; l++) {
             // global-memory smoothing of level l and restriction to l + 1 exist below the tail
@@ -378,6 +402,7 @@ int BatchImpl::rebuild() {
         if (d.solver == 0) {
             any_gs = true;
             max_gs_iters = std::max(max_gs_iters, d.iterations);
+            max_gs_cells = std::max<uint64_t>(max_gs_cells, d.nc);
         } else {
             any_pcg = true;
             if (mg) {
@@ -403,6 +428,7 @@ int BatchImpl::rebuild() {
     StageWork* ws[kStages];
     ws[0] = &w_parts; ws[1] = &w_tiles; ws[2] = &w_cells; ws[3] = &w_half; ws[4] = &w_faces; ws[5] = &w_chunks;
     ws[kStages - 1] = &w_lchunks;
+    ws[kStages - 2] = &w_gsu;
     for (int l = 0; l < kMaxLevels; l++) {
         ws[6 + l] = &pw.level[l];
         ws[6 + kMaxLevels + l] = &pw.coarse[l];
@@ -526,6 +552,8 @@ int BatchImpl::rebuild() {
         }
     }
     if (pw.any_mg && (e = mg_tail_attr(pw.tail_smem)) != cudaSuccess) return cuda_fail(e, "tail kernel attribute");
+    gs_stream = any_gs && gs_stream_for(max_gs_cells);
+    if (gs_stream && (e = gs_stream_attr()) != cudaSuccess) return cuda_fail(e, "streamed GS attribute");
     if (any_pcg && !d_bar) {
         // [0]: the persistent solve's barrier, [1]: the cooperative smoothing kernels'
         if ((e = cudaMalloc(&d_bar, 2 * sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
@@ -557,11 +585,13 @@ int BatchImpl::record_gs_part(cudaStream_t st) {
     return PXF_OK;
 }
 
-// The reference red-black GS: 2 x iterations launches over the level-0 system-cell lists (built
-// once per substep), or, with PXF_GS_DENSE=1, over every cell of one colour.
+// The reference red-black GS: on large grids streamed through shared memory, kGsIters
+// iterations per pass (pressure_stream.cu); otherwise 2 x iterations launches over the level-0
+// system-cell lists (built once per substep), or, with PXF_GS_DENSE=1, over every cell of one colour.
 cudaError_t BatchImpl::record_gs(cudaStream_t st) {
     static const bool dense = [] { const char* v = std::getenv("PXF_GS_DENSE"); return v && v[0] == '1'; }();
     cudaError_t e = cudaSuccess;
+    if (gs_stream && !dense) return launch_gs_stream(w_gsu, max_gs_iters, st);
     if (!dense && (e = launch_gs_lists(w_lchunks, st)) != cudaSuccess) return e;
     for (uint32_t it = 0; it < max_gs_iters; it++)
         for (uint32_t parity = 0; parity < 2; parity++) {
@@ -1100,6 +1130,28 @@ uint32_t coarse_chunk() {
     return cs;
 }
 
+// z planes of a streamed-GS unit (PXF_GS_ZS overrides: 8 .. 4096): 48 (six segments of a
+// 256-plane grid: about two waves of units on the GPU's SMs for the 512 x 256 x 256 dam break),
+// 16 on grids of at most 128 planes.
+uint32_t gs_segment_planes(uint32_t nz) {
+    static const uint32_t fixed = [] {
+        const char* v = std::getenv("PXF_GS_ZS");
+        const long k = v ? std::atol(v) : 0;
+        return (k >= 8 && k <= 4096) ? uint32_t(k) : 0u;
+    }();
+    if (fixed) return fixed;
+    return nz <= 128 ? 16u : 48u;
+}
+
+// The streamed red-black GS for batches whose largest red-black grid has at least 2^24 cells;
+// below that the list sweeps, whose working set stays in L2, are faster. PXF_GS_STREAM=0/1
+// (read at every batch rebuild) forces either.
+bool gs_stream_for(uint64_t cells) {
+    const char* v = std::getenv("PXF_GS_STREAM");
+    if (v && (v[0] == '0' || v[0] == '1')) return v[0] == '1';
+    return cells >= (uint64_t(1) << 24);
+}
+
 uint32_t level0_chunk() {
     static const uint32_t cs = chunk_env("PXF_L0_CHUNK", 5120);
     return cs;
@@ -1277,6 +1329,18 @@ int create_impl(const FluidCfg& cfg, uint32_t seed, double fps, const pxf_option
     d.lev[0].cs = opts.pressure_solver == PXF_PRESSURE_PCG ? level0_chunk() : level0_chunk_gs(d.nc);
     d.lev[0].list = reinterpret_cast<uint32_t*>(m + L.llist[0]);
     d.lev[0].lcnt = reinterpret_cast<uint32_t*>(m + L.llcnt[0]);
+    if (opts.pressure_solver != PXF_PRESSURE_PCG) {
+        uint32_t g[4];
+        gs_unit_grid(s->dims, g);
+        d.p_alt = reinterpret_cast<float*>(m + L.p_alt);
+        d.rhs = reinterpret_cast<float*>(m + L.rhs);
+        d.gs_cnt = reinterpret_cast<uint8_t*>(m + L.gs_cnt);
+        d.gs_flag = reinterpret_cast<uint32_t*>(m + L.gs_flag);
+        d.gs_ntx = g[0];
+        d.gs_nty = g[1];
+        d.gs_nzs = g[2];
+        d.gs_zs = g[3];
+    }
     if (opts.pressure_solver == PXF_PRESSURE_PCG) {
         d.x2 = reinterpret_cast<float2*>(m + L.x2);
         d.x64 = reinterpret_cast<double*>(m + L.x64);

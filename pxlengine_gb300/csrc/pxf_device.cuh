@@ -85,6 +85,13 @@ struct SimDev {
     int nlev;
     int tail;                // first level handled by the shared-memory tail kernel
     MgLevel lev[kMaxLevels];
+    // red-black GS streamed through shared memory (pressure_stream.cu): units of gs_ntx x gs_nty
+    // x-y tiles times z segments of gs_zs planes
+    float* p_alt;            // second pressure buffer (passes alternate between the two)
+    float* rhs;              // div * h * h / dt of the current substep
+    uint8_t* gs_cnt;         // non-solid neighbour count of each system cell, 0 elsewhere
+    uint32_t* gs_flag;       // per unit: its interior holds a system cell
+    uint32_t gs_ntx, gs_nty, gs_nzs, gs_zs;
 };
 
 // Work index of one stage over a batch: item i of the stage belongs to simulation s where

@@ -132,6 +132,17 @@ constexpr long long kBarrierCycles = 4000000000LL;   // about 2 s at the GB300's
 // One cooperative launch that runs the whole precision solve of a substep.
 int pcg_solve_grid(size_t smem);
 constexpr int kActCounters = 1 + 2 * kMaxLevelsK;
+// Reference red-black GS streamed through shared memory, kGsIters iterations per pass over HBM:
+// units of a kGsTileX x kGsTileY x-y tile (loaded with a halo of kGsHalo cells) and a z segment.
+constexpr int kGsIters = 2;
+constexpr int kGsHalo = 2 * kGsIters;
+constexpr int kGsLoadX = 64, kGsLoadY = 32;
+constexpr int kGsTileX = kGsLoadX - 2 * kGsHalo, kGsTileY = kGsLoadY - 2 * kGsHalo;
+uint32_t gs_segment_planes(uint32_t nz);   // z planes of a unit
+bool gs_stream_for(uint64_t cells);        // the streamed solve for a batch whose largest GS grid has `cells`
+cudaError_t gs_stream_attr();
+// set-up (p_alt, right-hand side, counts, unit flags), ceil(max_iters / kGsIters) passes, copy-back
+cudaError_t launch_gs_stream(const StageWork& units, uint32_t max_iters, cudaStream_t st);
 // Reference red-black GS over level-0 system-cell lists (lists first, then one launch per colour).
 cudaError_t launch_gs_lists(const StageWork& chunks, cudaStream_t st);
 cudaError_t launch_pressure_rb_list(const StageWork& chunks, uint32_t parity, uint32_t it, cudaStream_t st);
