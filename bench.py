@@ -1,11 +1,14 @@
 #!/usr/bin/env python3
 """FLIP liquid substep benchmark (particle-substeps/s on one GB300 per rank).
 
-Default workload (N=1): the large single dam break — bounds [[0,0,0],[1,0.5,0.5]] at
-resolution 256 (256 x 128 x 128 MAC grid, h = 1/256), fill [[0,0,0],[0.25,0.5,0.5]], 8 particles
-per cell seeded with the reference LCG (8,001,504 particles), zero initial velocity, gravity
--9.81, dt = 1/120 (fps 15, 8 substeps), FLIP 0.95, pressure by PCG with FP64 dot products, FP64
-solution and FP64 restart residuals to relative residual 1e-6.
+Default workload (N=1): the stress double dam break, the largest single-GPU configuration —
+bounds [[0,0,0],[2,1,1]] at resolution 512 (512 x 256 x 256 MAC grid, h = 1/256), two fluid
+boxes x in [0, 0.6] and [1.4, 2.0], y in [0, 0.6], full z, 8 particles per cell seeded with the
+reference LCG (95,126,400 particles), zero initial velocity, gravity -9.81, dt = 1/120 (fps 15,
+8 substeps), FLIP 0.95, the reference's red-black Gauss-Seidel pressure solve with 80 iterations,
+FP32 throughout. --config dam256 is the large single dam break with the precision solver (PCG
+with FP64 dot products and restarts to relative residual 1e-6); dam256_gs the same grid with the
+reference solver; dam64 the reference's own CPU-runnable case.
 
 A step is one substep of that simulation. `value` is device time of K substeps (CUDA events on
 the library's stream, inputs resident in HBM); `e2e` goes through the public C ABI with host
@@ -123,14 +126,27 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel from
-# one ncu capture of this workload, keyed by (config, kernel); the capture is summarised in profiles/.
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a kernel from one ncu
+# capture of this workload, keyed by (config, kernel); the captures are summarised in profiles/.
 KERNEL_TRAFFIC = {
     ("dam256", "k_p2g"): 408.48e6,
     ("dam256", "k_g2p"): 545.89e6,
     ("dam256", "k_pcg_update"): 30.11e6,
     ("dam256_gs", "k_pressure_rb_list"): 12.47e6,
 }
+# DRAM traffic per system cell of one launch, from a capture of a smaller grid, for kernels whose
+# traffic grows with the system cells (a full-size capture would exceed the profiler's size rules);
+# the traffic of a launch is this figure times the workload's system cells.
+KERNEL_TRAFFIC_PER_SYSTEM_CELL = {}
+
+
+def kernel_traffic(config, kernel, system_cells):
+    """DRAM bytes of one launch from a capture of this workload, else scaled from a smaller grid's
+    capture by the system cells; None when no capture covers the kernel."""
+    t = KERNEL_TRAFFIC.get((config, kernel))
+    if t is None and kernel in KERNEL_TRAFFIC_PER_SYSTEM_CELL:
+        t = KERNEL_TRAFFIC_PER_SYSTEM_CELL[kernel] * system_cells
+    return t
 
 
 def make_fluid(P, cfg):
@@ -139,12 +155,27 @@ def make_fluid(P, cfg):
                    particles_per_cell=cfg["ppc"], substeps=cfg["substeps"], pressure_iterations=cfg["iterations"])
 
 
+L2_BYTES = 129e6
+
+
+def state_bytes(dims, n):
+    """Device state one substep streams: particle records (current and sorted, 32 B each), the two
+    face velocity fields and the per-cell fields (13 B per cell)."""
+    nx, ny, nz = dims
+    C = nx * ny * nz
+    F = (nx + 1) * ny * nz + nx * (ny + 1) * nz + nx * ny * (nz + 1)
+    return 64 * n + 8 * F + 13 * C
+
+
 def workload_config(name, cfg, dims, n):
+    sb = state_bytes(dims, n)
+    l2 = (f"inputs larger than L2: {sb / 1e9:.2f} GB of particle and grid state per substep against 129 MB"
+          if sb > L2_BYTES else
+          f"working set inside L2 ({sb / 1e6:.0f} MB of particle and grid state): L2 not flushed between steps")
     return {"workload": f"dam_break_{name}", "grid": list(dims), "particles": n, "ppc": cfg["ppc"],
             "dt": f"1/{int(cfg['fps'] * cfg['substeps'])}", "pressure": (
                 "pcg_fp64dots_rtol1e-6" if cfg["solver"] == "pcg" else f"rbgs_{cfg['iterations']}"),
-            "seed": 0, "l2": "inputs larger than L2 (particle state 32 B x N, grid fields > 129 MB)",
-            "parallelism": "replicas"}
+            "seed": 0, "l2": l2, "parallelism": "replicas"}
 
 
 def kernel_bytes(kernel, N, F, C, Cf, lv=None):
@@ -171,6 +202,9 @@ def kernel_bytes(kernel, N, F, C, Cf, lv=None):
         "k_p2g": 32 * N + 8 * F + 4 * C,             # sorted particles and cell starts in; vel, vel_old out
         "k_divergence": 4 * F + 1 * C + 4 * C + 2 * C,   # faces, flags in; divergence, neighbour record out
         "k_pressure_rb": 8 * C,                      # one colour: 16C per red-black iteration
+        "k_gs_pass": 36 * Cf,                        # two red-black iterations of the system cells
+                                                     # (18 B per system cell per iteration, as above)
+        "k_gs_prep": 19 * C,                         # pressure, divergence, record in; p_alt, rhs, count out
         "k_pressure_rb_list": 9 * Cf,                # one colour of the system cells: list, record, div in,
                                                      # p out (14 B per colour cell), other colour's p in
         "k_pcg_dir": 22 * Cf,                        # list, z, p, record in; p', Ap out
@@ -189,7 +223,8 @@ def substep_bytes(N, F, C, Cf, solver, iters):
 
 
 def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1):
-    """The oracle (CPU restatement of the reference) on all host cores, one substep per step."""
+    """The oracle (CPU restatement of the reference) on all host cores, one substep per step,
+    starting from the seeded state."""
     import oracle
     threads = oracle.num_threads(0)
     fill = [{"min": list(a), "max": list(b)} for a, b in cfg["fill"]]
@@ -251,15 +286,14 @@ def divergence_linf(sim):
     return float(np.max(np.abs(d[fl])) * sim.dt) if fl.any() else 0.0
 
 
-def fp64_check(sim, cfg):
+def fp64_check(sim, origin, iterations):
     """One more substep of the GPU simulation against the oracle's FP64 solve of the same pressure
     system (the oracle's pre-pressure stages are bit-exact with the GPU's): max pressure error
     relative to max |p64|, and max |div v| * dt after the GPU's projection."""
     import numpy as np
     import oracle
     p0 = sim.read_particles()
-    o = oracle.OracleSim(sim.dims, sim.cell, sim.dt, 0.95, list(cfg["bounds"][0]), [0, -9.81, 0], cfg["iterations"],
-                         p0)
+    o = oracle.OracleSim(sim.dims, sim.cell, sim.dt, 0.95, list(origin), [0, -9.81, 0], iterations, p0)
     o.set_pressure("pcg64", rtol=1e-10, max_iter=100000)
     sim.step(1)
     for st in ("clear", "p2g", "normalize", "forces", "divergence", "pressure"):
@@ -328,6 +362,12 @@ def run_batched(args, world, rank, local):
     div = max(divergence_linf(s) for s in sims[:4])
     iters = [s.solver_stats()[0] for s in sims]
     b.close()
+    # FP64 reference of one more substep of the two smallest members (the oracle's FP64 solve)
+    fp64 = None
+    if rank == 0 and not args.no_fp64_check:
+        small = sorted(range(n), key=lambda i: int(np.prod(sims[i].dims)))[:2]
+        fp64 = [dict(member=i, grid=list(sims[i].dims), **fp64_check(sims[i], fl[i].bounds[0], fl[i].pressure_iterations))
+                for i in small]
     # the plain per-simulation loop on the same GPU: each simulation advanced alone, one after another
     for s in sims:
         s.step(1)
@@ -341,7 +381,8 @@ def run_batched(args, world, rank, local):
     for s in sims:
         s.close()
     return {"value": value, "value_local": value, "ms": ms, "lat": lat, "N": N, "cells": cells, "clk": clk, "tune": tune,
-            "div_linf": div, "iters": iters, "loop_value": loop_value, "loop_ms_per_round": loop_ms / loop_steps}
+            "div_linf": div, "iters": iters, "loop_value": loop_value, "loop_ms_per_round": loop_ms / loop_steps,
+            "fp64": fp64}
 
 
 def serve_request(P, rng, i):
@@ -404,16 +445,16 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="dam256", choices=sorted(CONFIGS) + ["batched", "serve"])
+    ap.add_argument("--config", default="dam512", choices=sorted(CONFIGS) + ["batched", "serve"])
     ap.add_argument("--batch-sims", type=int, default=64)
     ap.add_argument("--serve-rates", default="2,8")
     ap.add_argument("--serve-duration-s", type=float, default=15.0)
     ap.add_argument("--serve-drain-s", type=float, default=120.0)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=8, help="frames of the end-to-end measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
-    ap.add_argument("--fp64-check", action="store_true",
-                    help="after the run, compare one substep's pressure with the oracle's FP64 solve")
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="skip the comparison of one precision-solver substep's pressure with the oracle's FP64 solve")
     args = ap.parse_args()
     cfg = CONFIGS.get(args.config)
     rank = env_int("RANK", 0)
@@ -430,14 +471,17 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        r = cpu_baseline_run(cfg, args.steps, args.warmup)
+        # warm-up substeps on the CPU only load caches and pages: at most two, so that the run stays
+        # within a few minutes at 512 x 256 x 256 (about 5 s per substep on 16 cores)
+        r = cpu_baseline_run(cfg, args.steps, min(args.warmup, 2))
         line = {"metric": metric, "value": r["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded dam break, reference LCG seeding)",
                 "config": workload_config(args.config, cfg, r["dims"], r["particles"]),
                 "cpu_baseline": {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": "port",
-                                 "sample": "one full substep of the workload per step, all host threads"},
+                                 "sample": f"{args.steps} full substeps of the workload from the seeded state "
+                                           f"after {min(args.warmup, 2)} warm-up substeps, all host threads"},
                 "e2e": {"value": r["value"], "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -475,6 +519,7 @@ def main():
                                    "how": "each simulation advanced alone (own graph), one after another"},
                     "batched_over_loop": r["value_local"] / r["loop_value"], "autotune": r["tune"],
                     "divergence_linf_dt": r["div_linf"], "pcg_iterations": [min(r["iters"]), max(r["iters"])],
+                    "precision_vs_fp64": r["fp64"],
                     "clocks": r["clk"], "roofline": None, "cpu_baseline": None, "e2e": None}
             print(json.dumps(line), flush=True)
         if dist:
@@ -558,7 +603,7 @@ def main():
             per_launch = kernel_bytes(name, N, F, C, Cf, lv)
             achieved = per_launch / (tot / launches / 1e3) / 1e9
             roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": KERNEL_TRAFFIC.get((args.config, name)),
+                        "frac": achieved / peak, "traffic": kernel_traffic(args.config, name, Cf),
                         "peak_source": peak_src, "alg_bytes_per_launch": per_launch,
                         "launches_per_substep": launches, "avg_launch_us": 1e3 * tot / launches,
                         "share_of_substep": tot / total, "largest_kernel": ranked[0][0]}
@@ -610,8 +655,8 @@ def main():
     precision = None
     if cfg["solver"] == "pcg" and rank == 0:
         precision = {"divergence_linf_dt": divergence_linf(sim)}
-        if args.fp64_check:
-            precision = fp64_check(sim, cfg)
+        if not args.no_fp64_check:
+            precision = fp64_check(sim, cfg["bounds"][0], cfg["iterations"])
 
     launches_per_substep = sum(k["launches"] for k in kernels) if kernels else None
     solver_stats = None
@@ -621,9 +666,9 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r = cpu_baseline_run(cfg, 1, 0)
+        r = cpu_baseline_run(cfg, 2, 0)
         cpu = {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": "port",
-               "sample": "one full substep of the same workload (from the seeded state), all host threads"}
+               "sample": "two full substeps of the same workload from the seeded state, all host threads"}
 
     if rank == 0:
         line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
