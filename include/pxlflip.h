@@ -219,6 +219,16 @@ PXF_API int pxf_set_wait_timeout(pxf_sim* sim, double seconds);
  * the meshing's device time. */
 PXF_API int pxf_surface_mesh(pxf_sim* sim, uint32_t* vertices, uint32_t* triangles, int32_t* overflow,
                              double* device_ms);
+/* pxf_surface_mesh into the caller's device buffers, as the reference's s_verts / s_quads write
+ * the renderer's global buffers (fluid.slang:313-314, 343-351; fluid.rs:308-330): vertex idx goes
+ * to d_vertices[(vbase + idx) * 8 .. + 8] as (x, y, z, 0, nx, ny, nz, 0) floats, triangle t to
+ * d_indices[ibase + 3 t .. + 3] as vertex indices counted from vbase. max_vertices /
+ * max_triangles cap the writes (0: the fluid's max_triangles for both, like the reference); the
+ * returned counts and overflow flag follow the reference's capping. The library's own mesh
+ * buffers (pxf_read_mesh, pxf_mesh_device_buffers) are left as they were. */
+PXF_API int pxf_surface_mesh_into(pxf_sim* sim, float* d_vertices, uint32_t vbase, uint32_t max_vertices,
+                                  uint32_t* d_indices, uint32_t ibase, uint32_t max_triangles, uint32_t* vertices,
+                                  uint32_t* triangles, int32_t* overflow, double* device_ms);
 /* Surface grid of the simulation as FluidState::new sets it (fluid.rs:150-156): surface cells per
  * axis (grid cells x surface_refine), surface cell size, splat radius and iso level. */
 PXF_API int pxf_surface_info(const pxf_sim* sim, uint32_t dims[3], float* cell, float* radius, float* iso);
@@ -264,6 +274,26 @@ PXF_API void pxf_host_free(void* p);
  * shares the one scratch array, so calls whose work overlaps on the GPU race. */
 PXF_API int pxf_cell_starts_noalloc(const float* d_particles, uint32_t n, const uint32_t dims[3], const float origin[3],
                                     float h, uint32_t* d_cell_start, void* stream);
+
+/* ------------------------------------------------------------------ agent neighbour grid
+ * Counting sort of agents by hashed cell, the neighbour grid an agent simulation rebuilds every
+ * step (replaces grid_clear, grid_count, scan_local, scan_blocks, scan_add and grid_scatter,
+ * shaders/sim.slang:5-7, 28-104, driven by crates/pxl-render/src/sim.rs:230-260).
+ * d_agents: count records of stride_floats floats on the device, the position in the first three
+ * (the reference's Agent record is 16 floats). A cell is (floor(x / cs), floor(y / cs),
+ * floor(z / cs)) with cs = max(cell_size, 1e-6) and IEEE division, its hash
+ * ((cx * 73856093) ^ (cy * 19349663) ^ (cz * 83492791)) & (table_size - 1) in 32-bit unsigned
+ * arithmetic; table_size must be a power of two (pxf_grid_table_size gives the reference's choice).
+ * Outputs on the device: d_counts[table_size] agents per cell, d_offsets[table_size] their
+ * exclusive prefix sum (first slot of each cell) and d_sorted[count] the agent ids grouped by cell;
+ * inside one cell the ids' order is unspecified, as in the reference. d_scratch (device) holds at
+ * least pxf_grid_scratch_bytes(count, table_size) bytes; the call allocates nothing, queues its
+ * work on `stream` (a cudaStream_t; NULL = the default stream) and returns without waiting. */
+PXF_API uint32_t pxf_grid_table_size(uint32_t count);   /* (2 count).next_power_of_two() in [1024, 2^23], sim.rs:129 */
+PXF_API size_t pxf_grid_scratch_bytes(uint32_t count, uint32_t table_size);
+PXF_API int pxf_grid_sort(const float* d_agents, uint32_t stride_floats, uint32_t count, float cell_size,
+                          uint32_t table_size, uint32_t* d_offsets, uint32_t* d_counts, uint32_t* d_sorted,
+                          void* d_scratch, size_t scratch_bytes, void* stream);
 
 PXF_API void pxf_destroy(pxf_sim* sim);
 PXF_API const char* pxf_last_error(const pxf_sim* sim);

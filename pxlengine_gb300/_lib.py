@@ -111,6 +111,8 @@ def _sig():
         "pxf_set_wait_timeout": (C.c_int, [vp, C.c_double]),
         "pxf_surface_mesh": (C.c_int, [vp, u32p, u32p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
         "pxf_read_mesh": (C.c_int, [vp, vp, C.c_size_t, vp, C.c_size_t]),
+        "pxf_surface_mesh_into": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, vp, C.c_uint32, C.c_uint32, u32p, u32p,
+                                            C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
         "pxf_surface_info": (C.c_int, [vp, u32p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "pxf_mesh_device_buffers": (C.c_int, [vp, pp, pp]),
         "pxf_selftest_grid_barrier": (C.c_int, [C.c_uint32, C.c_int32, C.c_double, C.c_uint32, u32p]),
@@ -118,6 +120,10 @@ def _sig():
         "pxf_host_alloc": (C.c_int, [C.c_size_t, pp]),
         "pxf_host_free": (None, [vp]),
         "pxf_cell_starts_noalloc": (C.c_int, [vp, C.c_uint32, u32p, C.POINTER(C.c_float), C.c_float, vp, vp]),
+        "pxf_grid_table_size": (C.c_uint32, [C.c_uint32]),
+        "pxf_grid_scratch_bytes": (C.c_size_t, [C.c_uint32, C.c_uint32]),
+        "pxf_grid_sort": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, vp, vp, vp, vp, C.c_size_t,
+                                    vp]),
         "pxf_destroy": (None, [vp]),
         "pxf_last_error": (C.c_char_p, [vp]),
         "pxf_batch_create": (C.c_int, [pp]),

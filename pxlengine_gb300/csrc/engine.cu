@@ -1691,69 +1691,101 @@ int pxf_surface_info(const pxf_sim* s, uint32_t dims[3], float* cell, float* rad
     return PXF_OK;
 }
 
-int pxf_surface_mesh(pxf_sim* s, uint32_t* vertices, uint32_t* triangles, int32_t* overflow, double* device_ms) {
-    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
-    int rc = sim_wait(s);
-    if (rc) return rc;
+// The surface grid's working buffers and the library-owned mesh buffers (first meshing call).
+static int surface_buffers(pxf_sim* s) {
+    if (s->surf_mem) return PXF_OK;
     const FluidCfg& f = s->cfg;
     if (f.surface_refine == 0) return s->fail(PXF_EINVAL, "surface_refine must be at least 1");
+    SurfDev S = surface_params(s);
+    const uint64_t nn = uint64_t(S.sx + 1) * (S.sy + 1) * (S.sz + 1), sc = uint64_t(S.sx) * S.sy * S.sz;
+    if (nn >= (1ull << 32)) return s->fail(PXF_EINVAL, "surface grid too large (2^32 nodes)");
+    size_t off = 0;
+    auto take = [&](size_t b) { const size_t o = off; off += align256(b); return o; };
+    const size_t o_den = take(4 * nn), o_phi = take(4 * nn), o_cv = take(4 * sc);
+    const size_t o_v = take(size_t(S.max_verts) * 32), o_i = take(size_t(S.max_tris) * 12);
+    const size_t o_vc = take(4 * size_t(surface_chunks(sc))), o_qc = take(4 * size_t(surface_chunks(nn)));
+    const size_t o_ct = take(16);
+    void* mem = nullptr;
     cudaError_t e;
-    if (!s->surf_mem) {
-        SurfDev S = surface_params(s);
-        const uint64_t nn = uint64_t(S.sx + 1) * (S.sy + 1) * (S.sz + 1), sc = uint64_t(S.sx) * S.sy * S.sz;
-        if (nn >= (1ull << 32)) return s->fail(PXF_EINVAL, "surface grid too large (2^32 nodes)");
-        size_t off = 0;
-        auto take = [&](size_t b) { const size_t o = off; off += align256(b); return o; };
-        const size_t o_den = take(4 * nn), o_phi = take(4 * nn), o_cv = take(4 * sc);
-        const size_t o_v = take(size_t(S.max_verts) * 32), o_i = take(size_t(S.max_tris) * 12);
-        const size_t o_vc = take(4 * size_t(surface_chunks(sc))), o_qc = take(4 * size_t(surface_chunks(nn)));
-        const size_t o_ct = take(16);
-        void* mem = nullptr;
-        if ((e = cudaMalloc(&mem, off)) != cudaSuccess) {
-            cudaGetLastError();
-            return s->fail(PXF_ENOMEM, "surface buffers: " + std::to_string(off) + " bytes");
-        }
-        char* b = static_cast<char*>(mem);
-        S.density = reinterpret_cast<int32_t*>(b + o_den);
-        S.phi = reinterpret_cast<float*>(b + o_phi);
-        S.cell_vert = reinterpret_cast<uint32_t*>(b + o_cv);
-        S.verts = reinterpret_cast<float4*>(b + o_v);
-        S.indices = reinterpret_cast<uint32_t*>(b + o_i);
-        S.vchunk = reinterpret_cast<uint32_t*>(b + o_vc);
-        S.qchunk = reinterpret_cast<uint32_t*>(b + o_qc);
-        S.counters = reinterpret_cast<uint32_t*>(b + o_ct);
-        s->surf_mem = mem;
-        s->surf = S;
+    if ((e = cudaMalloc(&mem, off)) != cudaSuccess) {
+        cudaGetLastError();
+        return s->fail(PXF_ENOMEM, "surface buffers: " + std::to_string(off) + " bytes");
     }
+    char* b = static_cast<char*>(mem);
+    S.density = reinterpret_cast<int32_t*>(b + o_den);
+    S.phi = reinterpret_cast<float*>(b + o_phi);
+    S.cell_vert = reinterpret_cast<uint32_t*>(b + o_cv);
+    S.verts = reinterpret_cast<float4*>(b + o_v);
+    S.indices = reinterpret_cast<uint32_t*>(b + o_i);
+    S.vchunk = reinterpret_cast<uint32_t*>(b + o_vc);
+    S.qchunk = reinterpret_cast<uint32_t*>(b + o_qc);
+    S.counters = reinterpret_cast<uint32_t*>(b + o_ct);
+    s->surf_mem = mem;
+    s->surf = S;
+    return PXF_OK;
+}
+
+// Meshing with the given output view; the capped counts and the overflow flag as the reference
+// reads them back (fluid.rs:321-327).
+static int surface_run(pxf_sim* s, const SurfDev& S, uint32_t* vertices, uint32_t* triangles, int32_t* overflow,
+                       double* device_ms) {
     cudaStream_t st = sim_stream(s);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    e = launch_surface(s->surf, s->dev.posA, s->dev.np, st);
+    cudaError_t e = launch_surface(S, s->dev.posA, s->dev.np, st);
     cudaEventRecord(e1, st);
     if (e != cudaSuccess) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         return s->cuda_fail(e, "surface launch");
     }
-    rc = sim_wait(s);
+    int rc = sim_wait(s);
     float ms = 0;
     if (!rc) cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
     uint32_t cnt[2] = {0, 0};
-    if ((e = cudaMemcpy(cnt, s->surf.counters, 8, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    if ((e = cudaMemcpy(cnt, S.counters, 8, cudaMemcpyDeviceToHost)) != cudaSuccess)
         return s->cuda_fail(e, "surface counters");
-    const uint32_t mv = s->surf.max_verts, mt = s->surf.max_tris;
-    s->mesh_verts = std::min(cnt[0], mv);
-    s->mesh_tris = std::min(cnt[1], mt) / 2 * 2;
-    if (vertices) *vertices = s->mesh_verts;
-    if (triangles) *triangles = s->mesh_tris;
+    const uint32_t mv = S.max_verts, mt = S.max_tris;
+    if (vertices) *vertices = std::min(cnt[0], mv);
+    if (triangles) *triangles = std::min(cnt[1], mt) / 2 * 2;
     if (overflow) *overflow = (cnt[0] > mv || cnt[1] > mt) ? 1 : 0;
     if (device_ms) *device_ms = ms;
     return PXF_OK;
+}
+
+int pxf_surface_mesh(pxf_sim* s, uint32_t* vertices, uint32_t* triangles, int32_t* overflow, double* device_ms) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    int rc = sim_wait(s);
+    if (!rc) rc = surface_buffers(s);
+    if (rc) return rc;
+    uint32_t v = 0, t = 0;
+    if ((rc = surface_run(s, s->surf, &v, &t, overflow, device_ms))) return rc;
+    s->mesh_verts = v;
+    s->mesh_tris = t;
+    if (vertices) *vertices = v;
+    if (triangles) *triangles = t;
+    return PXF_OK;
+}
+
+int pxf_surface_mesh_into(pxf_sim* s, float* d_vertices, uint32_t vbase, uint32_t max_vertices, uint32_t* d_indices,
+                          uint32_t ibase, uint32_t max_triangles, uint32_t* vertices, uint32_t* triangles,
+                          int32_t* overflow, double* device_ms) {
+    if (!s) return set_global_error(PXF_EINVAL, "sim is NULL");
+    if (!d_vertices || !d_indices) return s->fail(PXF_EINVAL, "NULL vertex or index buffer");
+    int rc = sim_wait(s);
+    if (!rc) rc = surface_buffers(s);
+    if (rc) return rc;
+    SurfDev S = s->surf;
+    S.verts = reinterpret_cast<float4*>(d_vertices) + 2 * size_t(vbase);   // out_verts[(vbase + idx) * 2 + k]
+    S.indices = d_indices + size_t(ibase);                                   // out_indices[ibase + t * 3 + k]
+    if (max_vertices) S.max_verts = max_vertices;
+    if (max_triangles) S.max_tris = max_triangles;
+    return surface_run(s, S, vertices, triangles, overflow, device_ms);
 }
 
 int pxf_read_mesh(pxf_sim* s, float* vertices, size_t n_vertices, uint32_t* indices, size_t n_triangles) {

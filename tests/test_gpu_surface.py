@@ -63,3 +63,41 @@ def test_mesh_from_scene_json_matches_oracle(lib):
         out = s.surface_mesh()
         np.testing.assert_array_equal(out["vertices"], m["vertices"])
         np.testing.assert_array_equal(out["indices"], m["indices"])
+
+
+def test_mesh_into_caller_buffers(lib):
+    """pxf_surface_mesh_into writes the same mesh into the caller's device buffers at vbase / ibase
+    (fluid.slang:313-314, 343-351), indices counted from vbase, and touches nothing else."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    f = dam(res=32, ppc=8, iters=30)
+    with P.FluidState(f, fps=15.0) as s:
+        s.step(4)
+        o = _oracle_mesh(s, f, f.max_triangles)
+        nv, ni = len(o["vertices"]), len(o["indices"])
+        vbase, ibase = 37, 3 * 11
+        vb = torch.full(((vbase + nv + 5) * 8,), -7.0, dtype=torch.float32, device="cuda")
+        ib = torch.full((ibase + 3 * ni + 9,), -1, dtype=torch.int32, device="cuda")
+        for cap_v, cap_t in ((0, 0), (nv // 2, ni // 3)):
+            vb.fill_(-7.0)
+            ib.fill_(-1)
+            cv, ct, ov = C.c_uint32(), C.c_uint32(), C.c_int32()
+            rc = lib.pxf_surface_mesh_into(s.h, C.c_void_p(vb.data_ptr()), vbase, cap_v, C.c_void_p(ib.data_ptr()),
+                                           ibase, cap_t, C.byref(cv), C.byref(ct), C.byref(ov), None)
+            assert rc == 0, lib.pxf_last_error(s.h).decode()
+            v = vb.cpu().numpy().reshape(-1, 8)
+            i = ib.cpu().numpy().view(np.uint32)
+            if cap_v == 0:
+                assert (cv.value, ct.value, ov.value) == (nv, ni, 0)
+                np.testing.assert_array_equal(v[vbase:vbase + nv], o["vertices"])
+                np.testing.assert_array_equal(i[ibase:ibase + 3 * ni].reshape(-1, 3), o["indices"])
+            else:
+                o2 = oracle.surface_nets(s.read_particles(), s.surface_info()["dims"], s.surface_info()["cell"],
+                                         s.surface_info()["radius"], s.surface_info()["iso"], f.bounds[0],
+                                         cap_v, cap_t)
+                assert ov.value == 1 and cv.value == len(o2["vertices"]) and ct.value == len(o2["indices"])
+                np.testing.assert_array_equal(v[vbase:vbase + cv.value], o2["vertices"])
+                np.testing.assert_array_equal(i[ibase:ibase + 3 * ct.value].reshape(-1, 3), o2["indices"])
+            n_written = cv.value
+            assert (v[:vbase] == -7.0).all() and (v[vbase + n_written:] == -7.0).all()
+            assert (i[:ibase] == 0xFFFFFFFF).all()
