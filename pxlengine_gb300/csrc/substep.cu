@@ -754,8 +754,11 @@ __device__ __forceinline__ void face_taps(const SimDev& s, int c, float x, float
         if (a == c) g += 0.5f;
         b[a] = f2i(floorf(g));
         const float f = g - float(b[a]);
-        wt[a][0] = fmix(1.0f - f, f, 0.0f);
-        wt[a][1] = fmix(1.0f - f, f, 1.0f);
+        // fmix(1 - f, f, 0) and fmix(1 - f, f, 1) (fluid.slang's lerp weights) are exactly 1 - f
+        // and f: f = g - floor(g) is +0 <= f < 1 or NaN (never infinite), so f * 0 is +0 or NaN,
+        // (1 - f) * 0 likewise, and adding +0 to 1 - f (never -0) or to f changes no bit.
+        wt[a][0] = 1.0f - f;
+        wt[a][1] = f;
         d[a] = n[a] + (a == c) - 1;
     }
     const uint32_t fdx = uint32_t(d[0] + 1), fdy = uint32_t(d[1] + 1);
