@@ -86,7 +86,7 @@ __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0
 // ------------------------------------------------------------------ set-up of a solve
 // One block per unit: p_alt = pressure, rhs = div * h * h / dt and the non-solid neighbour count
 // of every system cell (0 elsewhere) over the unit's interior, and the unit's flag = does the
-// interior hold a system cell (fluid with a non-solid neighbour).
+// interior hold a system cell (fluid with a non-solid neighbour). One warp per x-row.
 __global__ void __launch_bounds__(256) k_gs_prep(Work w) {
     for (uint32_t item = blockIdx.x; item < w.total; item += gridDim.x) {
         const int si = find_sim(w, item);
@@ -95,8 +95,6 @@ __global__ void __launch_bounds__(256) k_gs_prep(Work w) {
         const Unit t = unit_of(s, u);
         const int xe = min(t.x0 + kTX, s.nx), ye = min(t.y0 + kTY, s.ny);
         const int wx = xe - t.x0, wy = ye - t.y0;
-        const uint32_t per = uint32_t(wx) * uint32_t(wy);
-        const uint32_t total = per * uint32_t(t.z1 - t.z0);
         const float h = s.h, dt = s.dt;
         const size_t nx = size_t(s.nx), nxy = nx * size_t(s.ny);
         const float* __restrict__ pr = s.pressure;
@@ -106,16 +104,21 @@ __global__ void __launch_bounds__(256) k_gs_prep(Work w) {
         float* __restrict__ rh = s.rhs;
         uint8_t* __restrict__ cn = s.gs_cnt;
         bool mine = false;
-        for (uint32_t k = threadIdx.x; k < total; k += blockDim.x) {
-            const uint32_t z = uint32_t(t.z0) + k / per, r = k % per;
-            const uint32_t y = uint32_t(t.y0) + r / uint32_t(wx), x = uint32_t(t.x0) + r % uint32_t(wx);
-            const size_t c = size_t(x) + nx * size_t(y) + nxy * size_t(z);
-            const uint32_t i = inf[c];
-            const bool sys = system_cell(i);
-            pa[c] = pr[c];
-            rh[c] = dv[c] * h * h / dt;
-            cn[c] = sys ? uint8_t((i >> 8) & 7u) : uint8_t(0);
-            mine |= sys;
+        // one warp per x-row of the interior, lanes along x
+        const uint32_t rows = uint32_t(wy) * uint32_t(t.z1 - t.z0);
+        const int lane = int(threadIdx.x) & 31;
+        for (uint32_t row = threadIdx.x >> 5; row < rows; row += blockDim.x >> 5) {
+            const uint32_t y = uint32_t(t.y0) + row % uint32_t(wy), z = uint32_t(t.z0) + row / uint32_t(wy);
+            const size_t c0 = size_t(t.x0) + nx * size_t(y) + nxy * size_t(z);
+            for (int x = lane; x < wx; x += 32) {
+                const size_t c = c0 + size_t(x);
+                const uint32_t i = inf[c];
+                const bool sys = system_cell(i);
+                pa[c] = pr[c];
+                rh[c] = dv[c] * h * h / dt;
+                cn[c] = sys ? uint8_t((i >> 8) & 7u) : uint8_t(0);
+                mine |= sys;
+            }
         }
         const int any = __syncthreads_or(mine);
         if (threadIdx.x == 0) s.gs_flag[u] = uint32_t(any != 0);
