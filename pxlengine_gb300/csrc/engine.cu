@@ -1130,9 +1130,10 @@ uint32_t coarse_chunk() {
     return cs;
 }
 
-// z planes of a streamed-GS unit (PXF_GS_ZS overrides: 8 .. 4096): 48 (six segments of a
-// 256-plane grid: about two waves of units on the GPU's SMs for the 512 x 256 x 256 dam break),
-// 16 on grids of at most 128 planes.
+// z planes of a streamed-GS unit (PXF_GS_ZS overrides: 8 .. 4096): 40, 16 on grids of at most 128
+// planes. On the 512 x 256 x 256 dam break (one block per SM, units of 56 x 24 cells times a
+// segment) 40 planes measured 14.9 ms per substep over the first 20 timed substeps and 16.0 over
+// 100, against 15.3 / 16.1 for 48, 16.8 for 64 and 14.8 / 16.7 for 80.
 uint32_t gs_segment_planes(uint32_t nz) {
     static const uint32_t fixed = [] {
         const char* v = std::getenv("PXF_GS_ZS");
@@ -1140,7 +1141,7 @@ uint32_t gs_segment_planes(uint32_t nz) {
         return (k >= 8 && k <= 4096) ? uint32_t(k) : 0u;
     }();
     if (fixed) return fixed;
-    return nz <= 128 ? 16u : 48u;
+    return nz <= 128 ? 16u : 40u;
 }
 
 // The streamed red-black GS for batches whose largest red-black grid has at least 2^24 cells;
