@@ -64,6 +64,16 @@ struct BatchImpl {
     StageWork w_lchunks;                 // level-0 system-cell list chunks (PCG and the list GS)
     StageWork w_gsu;                     // units of the streamed red-black GS
     bool gs_stream = false;              // the red-black GS of this batch is streamed (largest grid)
+    bool gs_res = false;                 // the red-black GS as one cooperative launch (pressure_resident.cu)
+    std::vector<GsResBlock> res_plan;    // its blocks
+    size_t res_smem = 0;
+    void* d_res = nullptr;               // plan, flags and error word of that launch
+    size_t cap_res = 0;
+    GsResBlock* d_res_plan = nullptr;
+    uint32_t* d_res_flags = nullptr;
+    uint32_t* d_res_err = nullptr;
+    long long res_limit = kBarrierCycles;
+    int res_skip = -1;
     PcgWork pw;                          // precision-solver work indexes
     uint32_t max_gs_iters = 0;
     bool any_gs = false, any_pcg = false;
@@ -285,6 +295,7 @@ BatchImpl::~BatchImpl() {
     if (d_flag) cudaFree(d_flag);
     if (h_flag) cudaFreeHost(h_flag);
     if (d_bar) cudaFree(d_bar);
+    if (d_res) cudaFree(d_res);
     if (d_tile_base) cudaFree(d_tile_base);
     if (ord.order) cudaFree(ord.order);
     if (ord.bucket) cudaFree(ord.bucket);
@@ -554,6 +565,27 @@ int BatchImpl::rebuild() {
     if (pw.any_mg && (e = mg_tail_attr(pw.tail_smem)) != cudaSuccess) return cuda_fail(e, "tail kernel attribute");
     gs_stream = any_gs && gs_stream_for(max_gs_cells);
     if (gs_stream && (e = gs_stream_attr()) != cudaSuccess) return cuda_fail(e, "streamed GS attribute");
+    gs_res = false;
+    if (any_gs && !gs_stream && gs_resident_for(max_gs_cells) && plan_gs_resident(host, res_plan, res_smem)) {
+        const size_t nb = res_plan.size();
+        const size_t plan_bytes = align256(nb * sizeof(GsResBlock));
+        const size_t flag_bytes = align256(nb * kGsResFlagStride * sizeof(uint32_t));
+        const size_t need = plan_bytes + flag_bytes + 256;
+        if (need > cap_res) {
+            if (d_res) cudaFree(d_res);
+            d_res = nullptr;
+            cap_res = need;
+            if ((e = cudaMalloc(&d_res, cap_res)) != cudaSuccess) return cuda_fail(e, "red-black solve plan");
+        }
+        d_res_plan = static_cast<GsResBlock*>(d_res);
+        d_res_flags = reinterpret_cast<uint32_t*>(static_cast<char*>(d_res) + plan_bytes);
+        d_res_err = reinterpret_cast<uint32_t*>(static_cast<char*>(d_res) + plan_bytes + flag_bytes);
+        if ((e = cudaMemcpy(d_res_plan, res_plan.data(), nb * sizeof(GsResBlock), cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (e = cudaMemset(d_res_err, 0, sizeof(uint32_t))) != cudaSuccess)
+            return cuda_fail(e, "red-black solve plan");
+        gs_res_knobs(res_limit, res_skip);
+        gs_res = true;
+    }
     if (any_pcg && !d_bar) {
         // [0]: the persistent solve's barrier, [1]: the cooperative smoothing kernels'
         if ((e = cudaMalloc(&d_bar, 2 * sizeof(GridBar))) != cudaSuccess) return cuda_fail(e, "grid barrier");
@@ -592,6 +624,9 @@ cudaError_t BatchImpl::record_gs(cudaStream_t st) {
     static const bool dense = [] { const char* v = std::getenv("PXF_GS_DENSE"); return v && v[0] == '1'; }();
     cudaError_t e = cudaSuccess;
     if (gs_stream && !dense) return launch_gs_stream(w_gsu, max_gs_iters, st);
+    if (gs_res && !dense)
+        return launch_gs_resident(d_sims, d_res_plan, int(res_plan.size()), d_res_flags, d_res_err, res_smem, res_limit,
+                                  res_skip, st);
     if (!dense && (e = launch_gs_lists(w_lchunks, st)) != cudaSuccess) return e;
     for (uint32_t it = 0; it < max_gs_iters; it++)
         for (uint32_t parity = 0; parity < 2; parity++) {
@@ -927,6 +962,15 @@ int BatchImpl::wait() {
         if ((persistent && hb[0].err) || (pw.sweep_bar && hb[1].err))
             return fail(PXF_ETIMEDOUT, "the pressure solve stopped: a grid barrier wait timed out");
     }
+    if (gs_res && d_res_err) {
+        uint32_t he = 0;
+        e = cudaMemcpy(&he, d_res_err, sizeof(he), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "red-black solve state");
+        if (he) {
+            cudaMemset(d_res_err, 0, sizeof(uint32_t));
+            return fail(PXF_ETIMEDOUT, "the red-black pressure solve stopped: a wait for a neighbouring block timed out");
+        }
+    }
     return PXF_OK;
 }
 
@@ -1151,6 +1195,28 @@ bool gs_stream_for(uint64_t cells) {
     const char* v = std::getenv("PXF_GS_STREAM");
     if (v && (v[0] == '0' || v[0] == '1')) return v[0] == '1';
     return cells >= (uint64_t(1) << 24);
+}
+
+// The red-black GS below the streamed threshold as one cooperative launch (pressure_resident.cu)
+// for batches whose largest red-black grid has at least 2^21 cells, where it fits: 1.66 against
+// 1.81 ms per substep at 256x128x128, but 0.41 against 0.35 ms at 64x32x32, where one launch per
+// colour costs less than the block-to-block waits. PXF_GS_RESIDENT=0/1 (read at every batch
+// rebuild) forces either.
+bool gs_resident_for(uint64_t cells) {
+    const char* v = std::getenv("PXF_GS_RESIDENT");
+    if (v && (v[0] == '0' || v[0] == '1')) return v[0] == '1';
+    return cells >= (uint64_t(1) << 21);
+}
+
+// Failure-path test knobs of that launch, read at every batch rebuild: PXF_GS_RES_LIMIT_MS bounds
+// each wait (default about 2 s), PXF_GS_RES_SKIP names a block that returns at once, so the blocks
+// that wait for it run out of time, set the error word and return.
+void gs_res_knobs(long long& limit_cycles, int& skip) {
+    const char* l = std::getenv("PXF_GS_RES_LIMIT_MS");
+    const double ms = l ? std::atof(l) : 0.0;
+    limit_cycles = (ms > 0.0 && ms <= 10000.0) ? (long long)(ms * 2.1e6) : kBarrierCycles;
+    const char* k = std::getenv("PXF_GS_RES_SKIP");
+    skip = k ? std::atoi(k) : -1;
 }
 
 uint32_t level0_chunk() {

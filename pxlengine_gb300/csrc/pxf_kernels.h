@@ -1,6 +1,7 @@
 // Host-visible launchers of the FLIP substep kernels (substep.cu, pcg.cu).
 #pragma once
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "pxf_device.cuh"
@@ -140,9 +141,23 @@ constexpr int kGsLoadX = 64, kGsLoadY = 32;
 constexpr int kGsTileX = kGsLoadX - 2 * kGsHalo, kGsTileY = kGsLoadY - 2 * kGsHalo;
 uint32_t gs_segment_planes(uint32_t nz);   // z planes of a unit
 bool gs_stream_for(uint64_t cells);        // the streamed solve for a batch whose largest GS grid has `cells`
+bool gs_resident_for(uint64_t cells);      // the one-launch red-black solve (largest GS grid of a batch)
+void gs_res_knobs(long long& limit_cycles, int& skip);
 cudaError_t gs_stream_attr();
 // set-up (p_alt, right-hand side, counts, unit flags), ceil(max_iters / kGsIters) passes, copy-back
 cudaError_t launch_gs_stream(const StageWork& units, uint32_t max_iters, cudaStream_t st);
+// Reference red-black GS as one cooperative launch whose blocks own fixed cell ranges and wait
+// only for the blocks within one z-plane of them (pressure_resident.cu).
+constexpr uint32_t kGsResFlagStride = 32;   // flag words between two blocks' flags (a 128-byte line each)
+struct GsResBlock {
+    uint32_t sim;          // simulation of the batch
+    uint32_t lo, hi;       // its cells [lo, hi)
+    uint32_t dep0, dep1;   // blocks [dep0, dep1) within one z-plane of those cells, this one included
+};
+bool plan_gs_resident(const std::vector<SimDev>& sims, std::vector<GsResBlock>& plan, size_t& smem);
+// Zeroes the flags, then the launch (2 x iterations half sweeps of every GS simulation).
+cudaError_t launch_gs_resident(const SimDev* sims, const GsResBlock* plan, int blocks, uint32_t* flags,
+                               uint32_t* err, size_t smem, long long limit_cycles, int skip, cudaStream_t st);
 // Reference red-black GS over level-0 system-cell lists (lists first, then one launch per colour).
 cudaError_t launch_gs_lists(const StageWork& chunks, cudaStream_t st);
 cudaError_t launch_pressure_rb_list(const StageWork& chunks, uint32_t parity, uint32_t it, cudaStream_t st);
