@@ -179,11 +179,12 @@ def workload_config(name, cfg, dims, n):
             "seed": 0, "l2": l2, "parallelism": "replicas"}
 
 
-def kernel_bytes(kernel, N, F, C, Cf, lv=None):
+def kernel_bytes(kernel, N, F, C, Cf, lv=None, iters=0):
     """Algorithmic bytes of one launch of a kernel: each array the kernel must touch counted once,
     4 B per face or cell value, 32 B per particle, 1 B per cell flag, 2 B per neighbour record,
     4 B per cell-list entry (Cf = system cells). Multigrid kernels: the mean over the launches of
-    one V-cycle, from the per-level system cells (lv)."""
+    one V-cycle, from the per-level system cells (lv). The one-launch red-black solve: all `iters`
+    iterations."""
     if kernel in ("k_mg_smooth", "k_mg_restrict"):
         if not lv or lv["tail"] <= 0:
             return None
@@ -208,6 +209,8 @@ def kernel_bytes(kernel, N, F, C, Cf, lv=None):
         "k_gs_prep": 19 * C,                         # pressure, divergence, record in; p_alt, rhs, count out
         "k_pressure_rb_list": 9 * Cf,                # one colour of the system cells: list, record, div in,
                                                      # p out (14 B per colour cell), other colour's p in
+        "k_gs_resident": 18 * Cf * iters,            # every red-black iteration in one launch, 18 B per
+                                                     # system cell per iteration as above
         "k_pcg_dir": 22 * Cf,                        # list, z, p, record in; p', Ap out
         "k_pcg_update": 38 * Cf,                     # list, p, Ap, r, x (8 B) in; r, x, red z out
         "k_project": 8 * F + 5 * C,                  # faces in and out; pressure, flags in
@@ -603,16 +606,16 @@ def main():
         kernels = []
         for n, k, m in prof:
             rec = {"kernel": n, "launches": k, "ms": m, "share": m / total}
-            b = kernel_bytes(n, N, F, C, Cf, lv)
+            b = kernel_bytes(n, N, F, C, Cf, lv, iters)
             if b:
                 gbs = b / (m / k / 1e3) / 1e9
                 rec.update({"alg_bytes_per_launch": b, "achieved_gbs": gbs, "frac_of_peak": gbs / peak})
             kernels.append(rec)
         ranked = sorted(prof, key=lambda r: -r[2])
-        top = next((r for r in ranked if kernel_bytes(r[0], N, F, C, Cf, lv)), None)
+        top = next((r for r in ranked if kernel_bytes(r[0], N, F, C, Cf, lv, iters)), None)
         if top:
             name, launches, tot = top
-            per_launch = kernel_bytes(name, N, F, C, Cf, lv)
+            per_launch = kernel_bytes(name, N, F, C, Cf, lv, iters)
             achieved = per_launch / (tot / launches / 1e3) / 1e9
             roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": kernel_traffic(args.config, name, Cf),
