@@ -133,6 +133,7 @@ KERNEL_TRAFFIC = {
     ("dam256", "k_g2p"): 545.89e6,
     ("dam256", "k_pcg_update"): 30.11e6,
     ("dam256_gs", "k_pressure_rb_list"): 12.47e6,
+    ("dam256_gs", "k_gs_resident"): 17.61e6,
     ("dam512", "k_gs_pass"): 211.6e6,
 }
 # DRAM traffic per system cell of one launch, from a capture of a smaller grid, for kernels whose
