@@ -1,0 +1,46 @@
+"""The oracle against the fixtures that pxlengine's own shader produced (tests/golden/ref_golden.npz,
+written by tests/golden/make_ref_golden.py from shaders/fluid.slang run on the CPU): the same
+seeded scenes through the oracle give the same bits. Runs everywhere; the GPU library meets the
+same fixtures in tests/test_gpu_reference_golden.py."""
+import os
+
+import numpy as np
+
+import oracle
+
+GOLD = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_golden.npz"))
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def test_dam_scene():
+    bounds = [[0, 0, 0], [1, 0.5, 0.5]]
+    dims, h = oracle.grid(bounds, 24)
+    assert dims == tuple(GOLD["dam_dims"])
+    p0 = oracle.seed_particles(bounds, 24, [{"min": [0, 0, 0], "max": [0.3, 0.4, 0.5]}], 4, 0)
+    assert np.array_equal(bits(p0), bits(GOLD["dam_initial"]))
+    o = oracle.OracleSim(dims, h, oracle.dt_for(24.0, 8), 0.95, bounds[0], [0, -9.81, 0], 80, p0)
+    o.step(8)
+    assert np.array_equal(bits(o.read(oracle.PARTICLES)), bits(GOLD["dam_particles"]))
+    assert np.array_equal(bits(o.read(oracle.PRESSURE)), bits(GOLD["dam_pressure"]))
+    assert np.array_equal(bits(o.read(oracle.VEL)), bits(GOLD["dam_vel"]))
+    assert np.array_equal(o.read(oracle.CELL_TYPE), GOLD["dam_cell_type"])
+    sh, radius, iso = (np.float32(v) for v in GOLD["dam_surface_params"])
+    m = oracle.surface_nets(GOLD["dam_particles"], GOLD["dam_surface_dims"], sh, radius, iso, [0, 0, 0],
+                           2_000_000, 2_000_000)
+    assert np.array_equal(bits(m["vertices"]), bits(GOLD["dam_vertices"]))
+    assert np.array_equal(m["indices"], GOLD["dam_indices"])
+
+
+def test_odd_scene():
+    bounds = [[0, 0, 0], [1.17, 0.71, 0.53]]
+    dims, h = oracle.grid(bounds, 25)
+    assert dims == tuple(GOLD["odd_dims"])
+    p0 = oracle.seed_particles(bounds, 25, [{"min": [0.05, 0.02, 0.03], "max": [0.6, 0.5, 0.5],
+                                             "velocity": [1.5, -0.5, 0.25]}], 2, 0)
+    o = oracle.OracleSim(dims, h, oracle.dt_for(24.0, 8), 0.6, bounds[0], [0, -9.81, 0], 7, p0)
+    o.step(5)
+    assert np.array_equal(bits(o.read(oracle.PARTICLES)), bits(GOLD["odd_particles"]))
+    assert np.array_equal(bits(o.read(oracle.PRESSURE)), bits(GOLD["odd_pressure"]))
