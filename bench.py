@@ -15,8 +15,10 @@ the library's stream, inputs resident in HBM); `e2e` goes through the public C A
 buffers: per step one pxf_write_particles from pinned memory, one pxf_advance_to_frame of a
 whole frame (`substeps` substeps) and one pxf_read_particles into pinned memory.
 
---impl reference times the CPU restatement of the reference algorithm (oracle/, OpenMP over all
-host cores) on the same workload; one step = one substep.
+--impl reference times the reference on the host cores (all threads) on the same workload, one
+step = one substep: pxlengine's own shaders/fluid.slang compiled for the CPU (oracle/_ref, built by
+oracle/ref_build.py) for the reference solver, the oracle's restatement (oracle/) where that build
+is absent and for the precision solver.
 Multi-GPU (torchrun): replicas only — every rank runs its own simulation, no exchange.
 """
 import argparse
@@ -227,28 +229,41 @@ def substep_bytes(N, F, C, Cf, solver, iters):
     return 96 * N + 60 * F + 40 * C + press
 
 
-def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1):
-    """The oracle (CPU restatement of the reference) on all host cores, one substep per step,
-    starting from the seeded state."""
+def cpu_baseline_run(cfg, steps, warmup, sample_substeps=1, budget_s=None):
+    """The reference on all host cores, one substep per step, from the seeded state: for the
+    reference solver pxlengine's own shaders/fluid.slang compiled for the CPU (oracle/_ref, kind
+    "reference") where it was built, else the oracle's restatement (kind "port"; also the precision
+    solver, which the reference does not have). With budget_s, the timed substeps are cut to what
+    fits that many seconds at the warm-up pace (at least two)."""
     import oracle
-    threads = oracle.num_threads(0)
+    from oracle import ref
     fill = [{"min": list(a), "max": list(b)} for a, b in cfg["fill"]]
-    dims, h = oracle.grid([list(cfg["bounds"][0]), list(cfg["bounds"][1])], cfg["resolution"])
-    p = oracle.seed_particles([list(cfg["bounds"][0]), list(cfg["bounds"][1])], cfg["resolution"], fill, cfg["ppc"], 0)
+    bounds = [list(cfg["bounds"][0]), list(cfg["bounds"][1])]
+    dims, h = oracle.grid(bounds, cfg["resolution"])
+    p = oracle.seed_particles(bounds, cfg["resolution"], fill, cfg["ppc"], 0)
     dt = oracle.dt_for(cfg["fps"], cfg["substeps"])
-    s = oracle.OracleSim(dims, h, dt, 0.95, list(cfg["bounds"][0]), [0, -9.81, 0], cfg["iterations"], p)
-    if cfg["solver"] == "pcg":
-        # the same algorithm as the GPU path: multigrid-preconditioned CG, FP64 dots and restarts
-        s.set_pressure("mgpcg", rtol=1e-6, max_iter=4000, restart=50)
+    if cfg["solver"] == "gs" and ref.available():
+        kind, threads = "reference", ref.num_threads(0)
+        s = ref.RefSim(dims, h, dt, 0.95, bounds[0], [0, -9.81, 0], cfg["iterations"], p)
+    else:
+        kind, threads = "port", oracle.num_threads(0)
+        s = oracle.OracleSim(dims, h, dt, 0.95, bounds[0], [0, -9.81, 0], cfg["iterations"], p)
+        if cfg["solver"] == "pcg":
+            # the same algorithm as the GPU path: multigrid-preconditioned CG, FP64 dots and restarts
+            s.set_pressure("mgpcg", rtol=1e-6, max_iter=4000, restart=50)
+    t0 = time.perf_counter()
     for _ in range(warmup):
         s.step(sample_substeps)
+    if budget_s and warmup:
+        pace = (time.perf_counter() - t0) / warmup
+        steps = max(2, min(steps, int(budget_s / max(pace, 1e-9))))
     t0 = time.perf_counter()
     for _ in range(steps):
         s.step(sample_substeps)
     el = time.perf_counter() - t0
     n = p.shape[0]
     return {"value": n * steps * sample_substeps / el, "ms_per_step": 1e3 * el / steps, "cores": threads,
-            "particles": n, "dims": dims}
+            "particles": n, "dims": dims, "kind": kind, "timed_steps": steps}
 
 
 # ------------------------------------------------------------------------------------ batched
@@ -462,6 +477,8 @@ def main():
     ap.add_argument("--serve-duration-s", type=float, default=15.0)
     ap.add_argument("--serve-drain-s", type=float, default=120.0)
     ap.add_argument("--e2e-steps", type=int, default=8, help="frames of the end-to-end measurement")
+    ap.add_argument("--reference-budget-s", type=float, default=150.0,
+                    help="--impl reference: timed substeps cut to fit this many seconds at the warm-up pace")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true",
@@ -484,15 +501,17 @@ def main():
             return
         # warm-up substeps on the CPU only load caches and pages: at most two, so that the run stays
         # within a few minutes at 512 x 256 x 256 (about 5 s per substep on 16 cores)
-        r = cpu_baseline_run(cfg, args.steps, min(args.warmup, 2))
+        r = cpu_baseline_run(cfg, args.steps, min(args.warmup, 2), budget_s=args.reference_budget_s)
         line = {"metric": metric, "value": r["value"], "unit": unit, "impl": "reference", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded dam break, reference LCG seeding)",
                 "config": workload_config(args.config, cfg, r["dims"], r["particles"]),
-                "cpu_baseline": {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": "port",
-                                 "sample": f"{args.steps} full substeps of the workload from the seeded state "
-                                           f"after {min(args.warmup, 2)} warm-up substeps, all host threads"},
+                "cpu_baseline": {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": r["kind"],
+                                 "sample": f"{r['timed_steps']} full substeps of the workload from the seeded state "
+                                           f"after {min(args.warmup, 2)} warm-up substeps, all host threads"
+                                           + (" (pxlengine's shaders/fluid.slang compiled for the CPU)"
+                                              if r["kind"] == "reference" else " (the oracle's restatement)")},
                 "e2e": {"value": r["value"], "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -683,8 +702,10 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r = cpu_baseline_run(cfg, 2, 0)
-        cpu = {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": "port",
-               "sample": "two full substeps of the same workload from the seeded state, all host threads"}
+        cpu = {"value": r["value"], "unit": unit, "cores": r["cores"], "kind": r["kind"],
+               "sample": "two full substeps of the same workload from the seeded state, all host threads"
+                         + (" (pxlengine's shaders/fluid.slang compiled for the CPU)" if r["kind"] == "reference"
+                            else " (the oracle's restatement)")}
 
     if rank == 0:
         line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,

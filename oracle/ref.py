@@ -1,7 +1,8 @@
 """ctypes binding of the reference runner (test infrastructure only): pxlengine's own
 shaders/fluid.slang compiled for the CPU by oracle/ref_build.py (oracle/_ref/libref_fluid.so).
-Available only where the reference checkout is (`available()`); the GPU tests use the fixtures
-that tests/golden/make_ref_golden.py wrote from it instead."""
+Available where the reference checkout is, or where a build made from it was carried along
+(`available()`); the GPU tests use the fixtures that tests/golden/make_ref_golden.py wrote from it.
+The substep's dispatches run on all host threads (OpenMP; integer atomics for InterlockedAdd)."""
 import ctypes as C
 
 import numpy as np
@@ -24,6 +25,8 @@ def load():
     lib.ref_sim_new.argtypes = [u32p, C.c_float, C.c_float, C.c_float, f32p, f32p, C.c_uint32, f32p, C.c_uint32]
     lib.ref_sim_new.restype = C.c_void_p
     lib.ref_sim_free.argtypes = [C.c_void_p]
+    lib.ref_num_threads.argtypes = [C.c_int]
+    lib.ref_num_threads.restype = C.c_int
     lib.ref_sim_stage.argtypes = [C.c_void_p, C.c_int]
     lib.ref_sim_stage.restype = C.c_int
     lib.ref_sim_step.argtypes = [C.c_void_p, C.c_uint32]
@@ -41,12 +44,16 @@ def available() -> bool:
     return load() is not None
 
 
+def num_threads(n: int = 0) -> int:
+    return load().ref_num_threads(n)
+
+
 STAGES = ("clear", "p2g", "normalize", "forces", "divergence", "pressure", "project", "g2p")
 ARRAYS = ("particles", "vel", "vel_old", "acc", "wacc", "cell_count", "cell_type", "pressure", "divergence")
 
 
 class RefSim:
-    """One simulation run by the reference's own kernels (FP32), one invocation at a time."""
+    """One simulation run by the reference's own kernels (FP32) on the host cores."""
 
     def __init__(self, dims, h, dt, flip, origin, gravity, iterations, particles):
         lib = load()

@@ -9,12 +9,16 @@
 // fluid_advance (fluid.rs:278-300: clear, p2g, normalize, forces, divergence, iterations x
 // {parity 0, 1} pressure_rb, project, g2p_advect) and the surface pass (fluid.rs:308-318:
 // s_clear, s_splat, s_phi, s_verts, s_quads), each dispatch as ceil(n / 256) groups of 256
-// invocations run one after another. Invocations of one dispatch do not depend on each other
-// except through InterlockedAdd (order-free integer sums) and, in s_verts / s_quads, the order in
-// which vertices and triangles take their slots: here ascending invocation index.
+// invocations. Invocations of one dispatch do not depend on each other except through
+// InterlockedAdd: integer sums (order-free; those dispatches run on all host threads, OpenMP) and,
+// in s_verts / s_quads, the order in which vertices and triangles take their slots (those two run
+// one invocation after another, in ascending index, the order the oracle and the library number
+// them in).
 #include <cstdint>
 #include <cstring>
 #include <vector>
+
+#include <omp.h>
 
 namespace ref {
 #include "fluid_slang.inc"
@@ -47,6 +51,12 @@ void bind(RefSim& s) {
 }
 
 template <class K> void dispatch(K kernel, uint64_t n) {
+    const int64_t total = int64_t(groups(n) * 256);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < total; i++) kernel(uint3(uint(i), 0u, 0u));
+}
+
+template <class K> void dispatch_in_order(K kernel, uint64_t n) {
     const uint64_t total = groups(n) * 256;
     for (uint64_t i = 0; i < total; i++) kernel(uint3(uint(i), 0u, 0u));
 }
@@ -110,6 +120,12 @@ void* ref_sim_new(const uint32_t dims[3], float h, float dt, float flip, const f
 }
 
 void ref_sim_free(void* p) { delete static_cast<RefSim*>(p); }
+
+// Host threads the dispatches use (n > 0 sets them first).
+int ref_num_threads(int n) {
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+}
 
 // Stages numbered as the oracle's: 0 clear, 1 p2g, 2 normalize, 3 forces, 4 divergence,
 // 5 pressure (every iteration), 6 project, 7 g2p.
@@ -181,8 +197,8 @@ int ref_surface_nets(const float* particles, uint32_t n, const uint32_t sdims[3]
     dispatch(ref::s_clear, snodes > scells ? snodes : scells);
     dispatch(ref::s_splat, n);
     dispatch(ref::s_phi, snodes);
-    dispatch(ref::s_verts, scells);
-    dispatch(ref::s_quads, snodes);
+    dispatch_in_order(ref::s_verts, scells);
+    dispatch_in_order(ref::s_quads, snodes);
     return 0;
 }
 

@@ -1,7 +1,6 @@
 // C++ stand-ins for the Slang/HLSL types and built-ins that pxlengine's shaders/fluid.slang uses,
-// so that the shader's own source compiles with g++ and its compute kernels run on the CPU, one
-// invocation at a time (test infrastructure only: oracle/ref_fluid.cpp, built by
-// oracle/ref_build.py into oracle/_ref/).
+// so that the shader's own source compiles with g++ and its compute kernels run on the CPU
+// (test infrastructure only: oracle/ref_fluid.cpp, built by oracle/ref_build.py into oracle/_ref/).
 //
 // Semantics chosen for the built-ins (the SPIR-V the reference's slangc emits calls
 // GLSL.std.450, whose results the Vulkan spec defines to these formulas or leaves open):
@@ -10,7 +9,8 @@
 //   max(a, b)      = a < b ? b : a,  min(a, b) = b < a ? b : a,  clamp(x, lo, hi) = min(max(x, lo), hi)
 //   int(f)         = truncation toward zero; floor / ceil / sqrt are the C library's (correctly
 //                    rounded, as SPIR-V's are exact for floor and ceil)
-//   InterlockedAdd = a plain add (invocations run one after another)
+//   InterlockedAdd = an atomic add (relaxed): the invocations of a dispatch may run on several
+//                    host threads; the add returns the value before it
 // Unsuffixed floating literals are float (g++ -fsingle-precision-constant), as in Slang.
 #pragma once
 #include <cmath>
@@ -113,11 +113,8 @@ inline float3 lerp(const float3& a, const float3& b, const float3& t) {
 inline float dot(const float3& a, const float3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float3 normalize(const float3& v) { return v / std::sqrt(dot(v, v)); }
 
-template <class T> void InterlockedAdd(T& dst, T v) { dst += v; }
-template <class T> void InterlockedAdd(T& dst, T v, T& original) {
-    original = dst;
-    dst += v;
-}
+template <class T> void InterlockedAdd(T& dst, T v) { __atomic_fetch_add(&dst, v, __ATOMIC_RELAXED); }
+template <class T> void InterlockedAdd(T& dst, T v, T& original) { original = __atomic_fetch_add(&dst, v, __ATOMIC_RELAXED); }
 
 template <class T>
 struct RWStructuredBuffer {
