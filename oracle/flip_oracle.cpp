@@ -16,13 +16,14 @@
 //   shaders/fluid.slang:222-355       surface nets: s_clear, s_splat, s_phi, s_verts, s_quads
 //   crates/pxl-render/src/fluid.rs:150-156, 308-330  surface grid, iso level, meshing schedule
 //
-// Parity status: partially pinned. The reference ships no numeric golden vectors and its
-// Slang/Vulkan path cannot run on these machines (no slangc, no Vulkan loader, no Rust
-// toolchain). Pinned: Fluid::grid against the reference's own unit test
-// (pxl-scene/src/lib.rs:886-899: [32,16,16], h = 0.0625), the dam-break particle count against
-// the reference's documentation (139k particles, docs/ROADMAP.md:83; 139,200 exactly), and the
-// seeding LCG against an independent pure-Python restatement (tests/golden/make_golden.py).
-// The kernel arithmetic is restated from the shader source; it is unpinned beyond that.
+// Parity status: pinned to the reference's own shader. tests/test_oracle_vs_reference.py runs
+// shaders/fluid.slang itself on the CPU (compiled by oracle/ref_build.py against
+// oracle/slang_shim.h, which binds its built-ins to the semantics below) beside this oracle and
+// finds the same bits after every stage of every substep and for the surface pass. The host
+// code the shader leaves to Rust (seeding, Fluid::grid, steps_for_frame) is pinned by the
+// reference's own unit test (pxl-scene/src/lib.rs:886-899: [32,16,16], h = 0.0625), the
+// dam-break particle count in its documentation (139k particles, docs/ROADMAP.md:83; 139,200
+// exactly) and an independent pure-Python restatement (tests/golden/make_golden.py).
 //
 // Semantics fixed here (the shader leaves them to the Slang compiler / Vulkan driver):
 //   lerp(a, b, t) = a*(1-t) + b*t      the GLSL.std.450 FMix definition that Slang lowers to

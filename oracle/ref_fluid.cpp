@@ -5,7 +5,8 @@
 // the SV_DispatchThreadID semantic are dropped, `out T x` parameters become `T& x`) and compiles
 // this file with oracle/slang_shim.h force-included. Every kernel below is the shader's own
 // function; this file only plays the host's part of crates/pxl-render/src/fluid.rs:
-// FluidPush from FluidState::new (fluid.rs:153-176), zeroed buffers, the substep schedule of
+// FluidPush from FluidState::new (fluid.rs:153-176), zeroed buffers (the reference allocates
+// them without initial data; zero is what the oracle and the library assume), the substep schedule of
 // fluid_advance (fluid.rs:278-300: clear, p2g, normalize, forces, divergence, iterations x
 // {parity 0, 1} pressure_rb, project, g2p_advect) and the surface pass (fluid.rs:308-318:
 // s_clear, s_splat, s_phi, s_verts, s_quads), each dispatch as ceil(n / 256) groups of 256
