@@ -134,6 +134,7 @@ KERNEL_TRAFFIC = {
     ("dam256", "k_p2g"): 408.48e6,
     ("dam256", "k_g2p"): 545.89e6,
     ("dam256", "k_pcg_update"): 30.11e6,
+    ("dam256", "k_mg_smooth"): 4.349e6,      # mean over the V-cycle's levels (500 launches)
     ("dam256_gs", "k_pressure_rb_list"): 12.47e6,
     ("dam256_gs", "k_gs_resident"): 17.61e6,
     ("dam512", "k_gs_pass"): 211.6e6,
