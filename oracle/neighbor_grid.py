@@ -9,6 +9,9 @@ Follows shaders/sim.slang:28-104 and crates/pxl-render/src/sim.rs:129,181:
 - grid_scatter (sim.slang:97-103): agent ids grouped by cell. The reference's order inside a cell
   follows its atomics; this restatement lists them in ascending id order.
 The division is IEEE float32 (numpy), the same operation the CUDA kernel uses.
+Pinned to the reference's own shader: tests/test_oracle_vs_reference.py runs sim.slang's grid
+kernels on the CPU (oracle/ref_sim.cpp) and finds the same offsets and counts and the same ids per
+cell.
 """
 import numpy as np
 

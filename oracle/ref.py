@@ -1,5 +1,6 @@
 """ctypes binding of the reference runner (test infrastructure only): pxlengine's own
-shaders/fluid.slang compiled for the CPU by oracle/ref_build.py (oracle/_ref/libref_fluid.so).
+shaders/fluid.slang and shaders/sim.slang compiled for the CPU by oracle/ref_build.py
+(oracle/_ref/libref_shaders.so).
 Available where the reference checkout is, or where a build made from it was carried along
 (`available()`); the GPU tests use the fixtures that tests/golden/make_ref_golden.py wrote from it.
 The substep's dispatches run on all host threads (OpenMP; integer atomics for InterlockedAdd)."""
@@ -36,6 +37,8 @@ def load():
                                      C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, u32p]
     lib.ref_surface_nets.restype = C.c_int
+    lib.ref_grid_sort.argtypes = [f32p, C.c_uint32, C.c_float, C.c_uint32, u32p, u32p, u32p]
+    lib.ref_grid_sort.restype = C.c_int
     _lib = lib
     return lib
 
@@ -117,3 +120,21 @@ def surface_nets(particles, sdims, sh, radius, iso, origin, max_verts, max_tris)
     nv, nt = min(cnt[0], max_verts), min(cnt[1], max_tris) // 2 * 2
     return {"density": den, "phi": phi, "cell_vert": cv, "vertices": verts[:nv], "indices": idx[:nt],
             "counts": (cnt[0], cnt[1])}
+
+
+def grid_sort(agents, cell_size, table_size):
+    """The reference's neighbour grid (sim.slang:32-104 with the dispatches of sim.rs:258-270) of
+    agents ([N, 16] float32 records, position first): (offsets, counts, sorted). The order of the
+    agents inside one cell follows the atomics of grid_scatter."""
+    lib = load()
+    assert lib is not None, "the reference checkout is not available"
+    a = np.ascontiguousarray(agents, dtype=np.float32).reshape(-1, 16)
+    n = a.shape[0]
+    offsets = np.zeros(table_size, dtype=np.uint32)
+    counts = np.zeros(table_size, dtype=np.uint32)
+    srt = np.zeros(max(n, 1), dtype=np.uint32)
+    u32p = C.POINTER(C.c_uint32)
+    rc = lib.ref_grid_sort(a.ctypes.data_as(C.POINTER(C.c_float)), n, float(cell_size), int(table_size),
+                           offsets.ctypes.data_as(u32p), counts.ctypes.data_as(u32p), srt.ctypes.data_as(u32p))
+    assert rc == 0, rc
+    return offsets, counts, srt[:n]

@@ -1,6 +1,7 @@
-// C++ stand-ins for the Slang/HLSL types and built-ins that pxlengine's shaders/fluid.slang uses,
-// so that the shader's own source compiles with g++ and its compute kernels run on the CPU
-// (test infrastructure only: oracle/ref_fluid.cpp, built by oracle/ref_build.py into oracle/_ref/).
+// C++ stand-ins for the Slang/HLSL types and built-ins that pxlengine's shaders/fluid.slang and
+// shaders/sim.slang use, so that the shaders' own source compiles with g++ and their compute
+// kernels run on the CPU (test infrastructure only: oracle/ref_fluid.cpp and oracle/ref_sim.cpp,
+// built by oracle/ref_build.py into oracle/_ref/).
 //
 // Semantics chosen for the built-ins (the SPIR-V the reference's slangc emits calls
 // GLSL.std.450, whose results the Vulkan spec defines to these formulas or leaves open):
@@ -11,10 +12,14 @@
 //                    rounded, as SPIR-V's are exact for floor and ceil)
 //   InterlockedAdd = an atomic add (relaxed): the invocations of a dispatch may run on several
 //                    host threads; the add returns the value before it
+//   GroupMemoryBarrierWithGroupSync = an OpenMP barrier: a workgroup's invocations run as one
+//                    team of host threads; groupshared arrays are plain arrays shared by the team
+//   saturate(v) = clamp(v, 0, 1) (NaN -> 0), cross = the usual determinant form, asuint = bit copy
 // Unsuffixed floating literals are float (g++ -fsingle-precision-constant), as in Slang.
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 typedef unsigned int uint;
 
@@ -77,6 +82,9 @@ struct float4 {
         struct {
             float x, y, z, w;
         };
+        struct {
+            float r, g, b, a;
+        };
         float3 xyz;
     };
     float4() = default;
@@ -84,6 +92,17 @@ struct float4 {
     float4(const float3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
     float& operator[](uint i) { return (&x)[i]; }
     float operator[](uint i) const { return (&x)[i]; }
+};
+
+inline float4 operator*(const float4& v, float s) { return float4(v.x * s, v.y * s, v.z * s, v.w * s); }
+inline float4 operator+(const float4& v, float s) { return float4(v.x + s, v.y + s, v.z + s, v.w + s); }
+
+struct uint4 {
+    uint x, y, z, w;
+    uint4() = default;
+    template <class A, class B, class C, class D>
+    uint4(A a, B b, C c, D d) : x(uint(a)), y(uint(b)), z(uint(c)), w(uint(d)) {}
+    explicit uint4(const float4& v) : x(uint(v.x)), y(uint(v.y)), z(uint(v.z)), w(uint(v.w)) {}
 };
 
 struct int2 {
@@ -112,6 +131,19 @@ inline float3 lerp(const float3& a, const float3& b, const float3& t) {
 }
 inline float dot(const float3& a, const float3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline float3 normalize(const float3& v) { return v / std::sqrt(dot(v, v)); }
+inline float3 cross(const float3& a, const float3& b) {
+    return float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline float abs(float v) { return std::fabs(v); }
+inline float saturate(float v) { return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f; }
+inline float4 saturate(const float4& v) { return float4(saturate(v.x), saturate(v.y), saturate(v.z), saturate(v.w)); }
+inline uint asuint(float v) {
+    uint u;
+    std::memcpy(&u, &v, 4);
+    return u;
+}
+inline uint4 asuint(const float4& v) { return uint4(asuint(v.x), asuint(v.y), asuint(v.z), asuint(v.w)); }
+inline void GroupMemoryBarrierWithGroupSync() { _Pragma("omp barrier") }
 
 template <class T> void InterlockedAdd(T& dst, T v) { __atomic_fetch_add(&dst, v, __ATOMIC_RELAXED); }
 template <class T> void InterlockedAdd(T& dst, T v, T& original) { original = __atomic_fetch_add(&dst, v, __ATOMIC_RELAXED); }
@@ -121,5 +153,7 @@ struct RWStructuredBuffer {
     T* p = nullptr;
     T& operator[](uint i) const { return p[i]; }
 };
+template <class T>
+using StructuredBuffer = RWStructuredBuffer<T>;
 template <class T>
 struct ConstantBuffer : T {};

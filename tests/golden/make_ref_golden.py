@@ -12,6 +12,9 @@ absent (tests/test_gpu_reference_golden.py):
   odd: bounds [[0,0,0],[1.17,0.71,0.53]], resolution 25, fill [0.05,0.02,0.03]..[0.6,0.5,0.5]
        moving at (1.5,-0.5,0.25), 2 particles per cell, seed 0, fps 24, 8 substeps per frame,
        FLIP 0.6, 7 iterations: particles and pressure after 5 substeps.
+  grid: the agents' neighbour grid (shaders/sim.slang:28-104) of 3,000 agents uniform in
+       [-2, 2]^3 (numpy seed 5), cell size 0.1, table 8,192: offsets, counts and the ids of each cell
+       in ascending order (the shader's own order inside a cell follows its atomics).
 Seeding is the oracle's restatement of fluid.rs:119-148 (itself checked against golden.json).
 
 Run (needs the reference checkout): python tests/golden/make_ref_golden.py
@@ -63,6 +66,16 @@ def main():
     out["odd_dims"] = np.array(dims, dtype=np.uint32)
     out["odd_particles"] = r.read("particles")
     out["odd_pressure"] = r.read("pressure")
+    rng = np.random.default_rng(5)
+    agents = np.zeros((3000, 16), dtype=np.float32)
+    agents[:, :3] = rng.uniform(-2, 2, (3000, 3)).astype(np.float32)
+    offs, cnts, srt = ref.grid_sort(agents, 0.1, 8192)
+    for h in np.nonzero(cnts)[0]:
+        srt[offs[h]:offs[h] + cnts[h]] = np.sort(srt[offs[h]:offs[h] + cnts[h]])
+    out["grid_positions"] = agents[:, :3].copy()
+    out["grid_offsets"] = offs
+    out["grid_counts"] = cnts
+    out["grid_sorted"] = srt
     np.savez_compressed(OUT, **out)
     print(OUT, os.path.getsize(OUT), "bytes")
 

@@ -48,3 +48,28 @@ def test_odd_scene(lib):
         s.step(5)
         assert np.array_equal(bits(s.read_particles()), bits(GOLD["odd_particles"]))
         assert np.array_equal(bits(s.read_grid("pressure")), bits(GOLD["odd_pressure"]))
+
+
+def test_neighbor_grid(lib):
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    pos = GOLD["grid_positions"]
+    n, table = pos.shape[0], 8192
+    rec = np.zeros((n, 16), dtype=np.float32)
+    rec[:, :3] = pos
+    d_rec = torch.from_numpy(rec).to("cuda")
+    off = torch.zeros(table, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(table, dtype=torch.int32, device="cuda")
+    srt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    sb = lib.pxf_grid_scratch_bytes(n, table)
+    scratch = torch.empty(sb, dtype=torch.uint8, device="cuda")
+    rc = lib.pxf_grid_sort(C.c_void_p(d_rec.data_ptr()), 16, n, C.c_float(0.1), table, C.c_void_p(off.data_ptr()),
+                           C.c_void_p(cnt.data_ptr()), C.c_void_p(srt.data_ptr()), C.c_void_p(scratch.data_ptr()),
+                           sb, None)
+    assert rc == 0, lib.pxf_last_error(None).decode()
+    torch.cuda.synchronize()
+    o, c, s = (t.cpu().numpy().view(np.uint32) for t in (off, cnt, srt))
+    assert np.array_equal(o, GOLD["grid_offsets"]) and np.array_equal(c, GOLD["grid_counts"])
+    for h in np.nonzero(c)[0]:
+        s[o[h]:o[h] + c[h]] = np.sort(s[o[h]:o[h] + c[h]])
+    assert np.array_equal(s, GOLD["grid_sorted"])

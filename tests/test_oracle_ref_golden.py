@@ -44,3 +44,10 @@ def test_odd_scene():
     o.step(5)
     assert np.array_equal(bits(o.read(oracle.PARTICLES)), bits(GOLD["odd_particles"]))
     assert np.array_equal(bits(o.read(oracle.PRESSURE)), bits(GOLD["odd_pressure"]))
+
+
+def test_neighbor_grid():
+    from oracle import neighbor_grid as NG
+    o, c, srt = NG.grid_sort(GOLD["grid_positions"], 0.1, 8192)
+    assert np.array_equal(o, GOLD["grid_offsets"]) and np.array_equal(c, GOLD["grid_counts"])
+    assert np.array_equal(srt, GOLD["grid_sorted"])

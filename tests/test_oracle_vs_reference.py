@@ -122,3 +122,25 @@ def test_committed_fixtures_come_from_the_runner(tmp_path, monkeypatch):
     assert sorted(fresh.files) == sorted(committed.files)
     for k in fresh.files:
         assert np.array_equal(fresh[k], committed[k]), k
+
+
+@pytest.mark.parametrize("n,cell_size,spread,table", [(0, 1.0, 1.0, 1024), (1, 0.5, 1.0, 1024), (5000, 0.01, 0.001, 16384),
+                                                       (40000, 0.05, 4.0, 131072), (70000, 0.0, 1.0, 262144),
+                                                       (200000, 0.5, 40.0, 1 << 19)])
+def test_neighbor_grid(n, cell_size, spread, table):
+    """The agents' neighbour grid of shaders/sim.slang:28-104 (grid_clear .. grid_scatter with the
+    dispatches of crates/pxl-render/src/sim.rs:258-270, workgroups as teams of host threads)
+    against oracle/neighbor_grid.py: offsets and counts equal, each cell's ids equal as a set
+    (grid_scatter's atomics order them)."""
+    from oracle import neighbor_grid as NG
+    rng = np.random.default_rng(n + 7)
+    a = np.zeros((n, 16), dtype=np.float32)
+    a[:, :3] = rng.uniform(-spread, spread, (n, 3)).astype(np.float32)
+    a[:, 3:] = np.float32(7.0)
+    ro, rc, rs = ref.grid_sort(a, cell_size, table)
+    wo, wc, ws = NG.grid_sort(a[:, :3], cell_size, table)
+    assert np.array_equal(ro, wo) and np.array_equal(rc, wc)
+    h = NG.cells(a[:, :3], cell_size, table)
+    assert np.array_equal(h[rs], np.repeat(np.arange(table, dtype=np.uint32), wc))
+    key = lambda s: np.sort(h[s].astype(np.int64) * (n + 1) + s)
+    assert np.array_equal(key(rs), key(ws))
