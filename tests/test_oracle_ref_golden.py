@@ -51,3 +51,21 @@ def test_neighbor_grid():
     o, c, srt = NG.grid_sort(GOLD["grid_positions"], 0.1, 8192)
     assert np.array_equal(o, GOLD["grid_offsets"]) and np.array_equal(c, GOLD["grid_counts"])
     assert np.array_equal(srt, GOLD["grid_sorted"])
+
+
+def test_digests_of_the_benchmark_workloads():
+    """The oracle reproduces the reference shader's digests on 64 x 32 x 32 after 200 substeps and
+    256 x 128 x 128 after 2 (tests/golden/ref_hashes.json)."""
+    import hashlib
+    import json
+    hashes = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_hashes.json")))
+    for name, res in (("dam64", 64), ("dam256_gs", 256)):
+        want = hashes[name]
+        b = [[0, 0, 0], [1, 0.5, 0.5]]
+        dims, h = oracle.grid(b, res)
+        p0 = oracle.seed_particles(b, res, [{"min": [0, 0, 0], "max": [0.25, 0.5, 0.5]}], 8, 0)
+        o = oracle.OracleSim(dims, h, oracle.dt_for(15.0, 8), 0.95, b[0], [0, -9.81, 0], 80, p0)
+        o.step(want["substeps"])
+        dig = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+        assert dig(o.read(oracle.PARTICLES)) == want["sha256_particles"], name
+        assert dig(o.read(oracle.PRESSURE)) == want["sha256_pressure"], name
