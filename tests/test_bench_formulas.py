@@ -51,3 +51,22 @@ def test_whole_job_rate():
     # two ranks of N particles, 100 substeps, the slowest rank 500 ms
     assert bench.whole_job_rate(2 * N, 100, 500.0) == pytest.approx(2 * N * 100 / 0.5)
     assert bench.over_ranks(None, 3.5) == 3.5
+
+
+def test_streamed_and_one_launch_red_black_kernels():
+    # a streamed pass is two iterations; the one-launch solve is every iteration of the substep
+    assert bench.kernel_bytes("k_gs_pass", N, F, C, CF) == 36 * CF
+    assert bench.kernel_bytes("k_gs_resident", N, F, C, CF, None, 80) == 18 * CF * 80
+    assert bench.kernel_bytes("k_gs_prep", N, F, C, CF) == 19 * C
+
+
+def test_reference_arm_sample_on_the_cpu():
+    """The CPU reference of a small workload: the reference's own shader where it was built
+    (kind "reference"), the oracle port otherwise; with a time budget the timed substeps shrink
+    to what fits it at the warm-up pace, never below two."""
+    from oracle import ref
+    r = bench.cpu_baseline_run(bench.CONFIGS["dam64"], 3, 1, budget_s=1e-6)
+    assert r["kind"] == ("reference" if ref.available() else "port")
+    assert r["timed_steps"] == 2 and r["particles"] == 108_000 and r["value"] > 0
+    p = bench.cpu_baseline_run(dict(bench.CONFIGS["dam64"], solver="pcg"), 1, 0)
+    assert p["kind"] == "port"
