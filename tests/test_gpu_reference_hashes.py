@@ -2,7 +2,8 @@
 reference-solver workloads (tests/golden/ref_hashes.json, written by
 tests/golden/make_ref_hashes.py from shaders/fluid.slang run on the CPU): 64 x 32 x 32 after 200
 substeps, 256 x 128 x 128 after 2 and the 512 x 256 x 256 double dam break after 1 — particles and
-pressure, bit for bit (SHA-256 of the float32 bytes)."""
+pressure, bit for bit (SHA-256 of the float32 bytes) — and the reference's example scene after 24
+frames, surface mesh included."""
 import hashlib
 import json
 import os
@@ -33,3 +34,19 @@ def test_workload_matches_reference(lib, name):
         parts = s.read_particles()
         assert digest(parts) == want["sha256_particles"], f"first particle {parts[0]} vs {want['first_particle']}"
         assert digest(s.read_grid("pressure")) == want["sha256_pressure"]
+
+
+def test_example_scene_24_frames_from_json(lib):
+    """The reference's example scene through the scene-JSON front end (bench.py's
+    DAM_BREAK_SCENE: render fps 24, seed 0): 24 frames of 8 substeps, then the surface mesh, the
+    same bits as the reference's shader (particles, pressure, vertex records, triangles)."""
+    want = HASHES["scene"]
+    with P.FluidState.from_json(bench.DAM_BREAK_SCENE) as s:
+        assert list(s.dims) == want["dims"] and s.particle_count() == want["particles"]
+        s.step(want["substeps"])
+        assert digest(s.read_particles()) == want["sha256_particles"]
+        assert digest(s.read_grid("pressure")) == want["sha256_pressure"]
+        m = s.surface_mesh()
+        assert len(m["vertices"]) == want["mesh_vertices"] and len(m["indices"]) == want["mesh_triangles"]
+        assert digest(m["vertices"]) == want["sha256_vertices"]
+        assert digest(m["indices"].astype(np.uint32)) == want["sha256_indices"]

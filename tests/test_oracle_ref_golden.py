@@ -69,3 +69,26 @@ def test_digests_of_the_benchmark_workloads():
         dig = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
         assert dig(o.read(oracle.PARTICLES)) == want["sha256_particles"], name
         assert dig(o.read(oracle.PRESSURE)) == want["sha256_pressure"], name
+
+
+def test_example_scene_digests():
+    """The oracle reproduces the reference shader's example scene after 24 frames (192 substeps)
+    and its surface mesh (tests/golden/ref_hashes.json)."""
+    import hashlib
+    import json
+    want = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                       "ref_hashes.json")))["scene"]
+    dig = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    b = [[-1, 0, -0.5], [1, 1.2, 0.5]]
+    dims, h = oracle.grid(b, 64)
+    p0 = oracle.seed_particles(b, 64, [{"min": [-0.97, 0.03, -0.47], "max": [-0.35, 0.95, 0.47]}], 8, 0)
+    o = oracle.OracleSim(dims, h, oracle.dt_for(24.0, 8), 0.95, b[0], [0, -9.81, 0], 80, p0)
+    o.step(want["substeps"])
+    parts = o.read(oracle.PARTICLES)
+    assert dig(parts) == want["sha256_particles"] and dig(o.read(oracle.PRESSURE)) == want["sha256_pressure"]
+    sh = np.float32(np.float32(h) / np.float32(2))
+    radius = np.float32(np.float32(2.0) * sh)
+    x = np.float32(radius / np.float32(h))
+    iso = np.float32(np.float32(0.5) * np.float32(8) * np.float32(np.float32(0.638) * np.float32(x * x * x)))
+    m = oracle.surface_nets(parts, [d * 2 for d in dims], sh, radius, iso, b[0], 2_000_000, 2_000_000)
+    assert dig(m["vertices"]) == want["sha256_vertices"] and dig(m["indices"]) == want["sha256_indices"]
